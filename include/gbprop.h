@@ -1,0 +1,151 @@
+/*
+ * gbprop.h -- C ABI of libgbprop, the GB300 (sm_103a) implementation of
+ * pyprop's pAMP x TensorPotential propagation step.
+ *
+ * Plain C types only: device pointers are `void*`, complex numbers are
+ * interleaved (re, im) pairs of double (complex128) or float (complex64),
+ * streams are passed as `void*` (a cudaStream_t; NULL = legacy default stream).
+ * Every call returns a gbprop_status; gbprop_last_error() gives the message of
+ * the most recent failure on the calling thread.
+ *
+ * Layout conventions (the reference's own):
+ *   wavefunction   psi[l][r], C order, radial index fastest, nl*nr complex
+ *                  (Wavefunction<2> data, core/wavefunction.h:11-116)
+ *   band storage   BLAS general band, element (i,j) at j*(2kb+1) + kb + i - j
+ *                  (GeometryInfoCommonBandedNonHermitian, pyprop/tensorpotential/GeometryInfo.py:407-459)
+ *   overlap factor upper band, element U(i,j) at j*(kd+1) + kd + i - j
+ *                  (OverlapMatrix::OverlapCholeskyUpper, core/representation/overlapmatrix.cpp:22-37)
+ *   angular pairs  int32 (row, col) per stored potential slot
+ *                  (GeometryInfoReducedSphHarmSelectionRule.GetBasisPairs,
+ *                   pyprop/tensorpotential/basis/ReducedSphericalHarmonic.py:22-37)
+ */
+#ifndef GBPROP_H
+#define GBPROP_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBPROP_OK = 0,
+    GBPROP_EINVAL = 1,       /* bad argument (sizes, null pointers, state) */
+    GBPROP_ECUDA = 2,        /* a CUDA runtime call failed */
+    GBPROP_EBREAKDOWN = 3,   /* informational: happy breakdown happened in the last step */
+    GBPROP_ENONFINITE = 4,   /* NaN/Inf seen in the Krylov norms */
+    GBPROP_ETIMEOUT = 5,     /* a bounded device-side wait gave up */
+    GBPROP_ELU = 6,          /* the Pade denominator was singular (pamp.h:544-550) */
+    GBPROP_EUNSUPPORTED = 7  /* storage/precision combination not provided */
+} gbprop_status;
+
+typedef enum {
+    GBPROP_FP64 = 0,         /* complex128 everywhere (the drop-in) */
+    GBPROP_FP32_MIXED = 1    /* complex64 basis + matvec, FP64 reductions/expm/state update */
+} gbprop_precision;
+
+typedef enum {
+    GBPROP_STORAGE_DIAG = 0, /* angular "Diag": one band per l, row = col = l */
+    GBPROP_STORAGE_IDENT = 1,/* angular "Ident": one band for every l */
+    GBPROP_STORAGE_SIMP = 2  /* angular "Simp": one band per (row, col) pair */
+} gbprop_storage;
+
+typedef struct gbprop_ctx* gbprop_handle;
+
+/* Counters as pAMP keeps them (pamp.h:121-124, PampWrapper::GetOperatorCount ...). */
+typedef struct {
+    long long operator_count;
+    long long inner_product_count;
+    long long orthogonalization_count;
+    long long breakdown_count;
+    long long step_count;
+    int last_basis_size;      /* Krylov vectors built in the last step */
+    int last_scaling_order;   /* s of the last scaling-and-squaring */
+    double error_estimate;    /* |y[m-1]|^2 of the last step (pamp.h:207-210,666) */
+} gbprop_stats;
+
+/* Library / device ---------------------------------------------------------- */
+const char* gbprop_version(void);
+const char* gbprop_last_error(void);
+/* Number of kernel launches made by this process since load (all handles). */
+long long gbprop_launch_count(void);
+
+/* Propagator handle: replaces core.krylov_PampWrapper_<Rank> (Boost.Python,
+ * core/krylov/pamp/pampwrapper.h:15-123) + the TensorPotential list of
+ * BasisPropagator (pyprop/tensorpotential/BasisPropagator.py:41-108).
+ *   krylov_basis_size       config key krylov_basis_size (pampwrapper.cpp:53)
+ *   exponentiation_method   krylov_exponentiation_method (pampwrapper.cpp:56-61); 0 = Pade only
+ *   double_orthogonalization krylov_double_orthogonalization (pampwrapper.cpp:64-69)
+ * stream: the CUDA stream every call of this handle is ordered on. */
+gbprop_status gbprop_create(gbprop_handle* out, int nl, int nr, int precision,
+                            int krylov_basis_size, int exponentiation_method,
+                            int double_orthogonalization, void* stream);
+gbprop_status gbprop_destroy(gbprop_handle h);
+
+/* Overlap Cholesky factor U (S = U^T U) of the radial rank, HOST pointer,
+ * upper band storage (nr, kd+1) of real values (OverlapCholeskyUpper is real
+ * for a real B-spline basis). Replaces OverlapMatrix::Setup (overlapmatrix.cpp:9-37). */
+gbprop_status gbprop_set_overlap(gbprop_handle h, int kd, const double* U_band);
+
+/* Add one consolidated TensorPotential (TensorPotential.py:33-87) in the
+ * reference storage, HOST pointers:
+ *   storage        gbprop_storage of the angular rank; the radial rank is BandNH
+ *   npairs         number of stored angular slots (nl for Diag, 1 for Ident)
+ *   pairs          (npairs, 2) int32 (row, col); NULL for Diag/Ident
+ *   kb             band half-width of the radial BandNH storage (order - 1)
+ *   data           (npairs, (2kb+1)*nr) complex128 interleaved (PotentialData)
+ *   time_dependent 1 if the potential is scaled by its time function
+ * dest[row] += scaling * data[pair] * src[col]   (generator.py:352). */
+gbprop_status gbprop_add_potential(gbprop_handle h, int storage, int npairs, const int* pairs,
+                                   int kb, const double* data, int time_dependent);
+
+/* Build device tables (solve coupling tables, band slots); call once after the
+ * overlap and all potentials are set.  Replaces PamPropagator.SetupStep /
+ * PampWrapper::Setup (PamPropagator.py:29-45, pampwrapper.cpp:74-81). */
+gbprop_status gbprop_finalize(gbprop_handle h);
+
+/* PamPropagator.AdvanceStep (PamPropagator.py:50-57) + PampWrapper::AdvanceStep
+ * (pampwrapper.cpp:84-108) for nsteps consecutive steps, on a DEVICE
+ * wavefunction psi (complex128 for FP64, complex64 for FP32_MIXED), in place:
+ *   psi <- U^-1 pAMP_m(U psi, dt; H(t_n))   for n = 0..nsteps-1
+ * scalings[n] (HOST array) is the time function at the start of step n
+ * (TensorPotential.py:98-100 with t = PropagatedTime).  dt may be complex
+ * (imaginary time).  Asynchronous on the handle's stream. */
+gbprop_status gbprop_advance(gbprop_handle h, void* psi, int nsteps, const double* scalings,
+                             double dt_re, double dt_im);
+
+/* Same as gbprop_advance on a HOST wavefunction: copies psi to the device,
+ * advances, copies it back and synchronises the stream. */
+gbprop_status gbprop_advance_host(gbprop_handle h, void* psi_host, int nsteps, const double* scalings,
+                                  double dt_re, double dt_im);
+
+/* BasisPropagator.MultiplyHamiltonianBalancedOverlap (BasisPropagator.py:131-159)
+ * when balanced != 0: dst = U^-H H(t) U^-1 src; otherwise
+ * MultiplyHamiltonianNoOverlap (:126-129): dst = H(t) src.  DEVICE pointers of
+ * the handle's precision; src is not modified. */
+gbprop_status gbprop_matvec(gbprop_handle h, const void* src, void* dst, double scaling, int balanced);
+
+/* CombinedRepresentation::MultiplySqrtOverlap(false) / SolveSqrtOverlap(conj)
+ * (combinedrepresentation.cpp:207-238), in place on a DEVICE wavefunction. */
+gbprop_status gbprop_multiply_sqrt_overlap(gbprop_handle h, void* psi);
+gbprop_status gbprop_solve_sqrt_overlap(gbprop_handle h, int conj, void* psi);
+
+gbprop_status gbprop_get_stats(gbprop_handle h, gbprop_stats* out);
+gbprop_status gbprop_reset_stats(gbprop_handle h);
+/* Copy the last step's (scaled, -i*dt*H) Hessenberg matrix, m*m complex128
+ * row-major, to HOST memory (pAMP::GetHessenbergMatrix, pamp.h:197-200). */
+gbprop_status gbprop_get_hessenberg(gbprop_handle h, double* out);
+gbprop_status gbprop_synchronize(gbprop_handle h);
+
+/* Stateless kernel ABI: TensorPotentialMultiply_<S0>_BandNH
+ * (generator.py:1373-1426 Fortran entry, :1486-1495 C++ wrapper,
+ *  TensorPotential.py:106-112 Python call), complex128 DEVICE buffers:
+ *   dst[row, :] += scaling * V[pair] (band) src[col, :]
+ * storage: GBPROP_STORAGE_DIAG (V is (nl, (2kb+1)*nr), pairs ignored) or
+ * GBPROP_STORAGE_SIMP (V is (npairs, (2kb+1)*nr), pairs (npairs, 2) int32 DEVICE). */
+gbprop_status gbprop_tensor_multiply_bandnh(int storage, const void* V, int npairs, const int* pairs,
+                                            int kb, double scaling, const void* src, void* dst,
+                                            int nl, int nr, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBPROP_H */

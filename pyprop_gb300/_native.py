@@ -1,0 +1,196 @@
+"""ctypes binding of libgbprop (include/gbprop.h).
+
+The library is built in-tree by pyprop_gb300/csrc/build.py.  Loading fails
+loudly when it is missing: there is no CPU fallback for the propagation path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgbprop.so")
+
+GBPROP_OK = 0
+STATUS_NAMES = {
+    0: "GBPROP_OK", 1: "GBPROP_EINVAL", 2: "GBPROP_ECUDA", 3: "GBPROP_EBREAKDOWN",
+    4: "GBPROP_ENONFINITE", 5: "GBPROP_ETIMEOUT", 6: "GBPROP_ELU", 7: "GBPROP_EUNSUPPORTED",
+}
+FP64 = 0
+FP32_MIXED = 1
+STORAGE_DIAG = 0
+STORAGE_IDENT = 1
+STORAGE_SIMP = 2
+
+
+class GbpropError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("operator_count", C.c_longlong),
+        ("inner_product_count", C.c_longlong),
+        ("orthogonalization_count", C.c_longlong),
+        ("breakdown_count", C.c_longlong),
+        ("step_count", C.c_longlong),
+        ("last_basis_size", C.c_int),
+        ("last_scaling_order", C.c_int),
+        ("error_estimate", C.c_double),
+    ]
+
+
+_lib = None
+
+# name -> (restype, argtypes)
+_PROTOS = {
+    "gbprop_version": (C.c_char_p, []),
+    "gbprop_last_error": (C.c_char_p, []),
+    "gbprop_launch_count": (C.c_longlong, []),
+    "gbprop_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "gbprop_destroy": (C.c_int, [C.c_void_p]),
+    "gbprop_set_overlap": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "gbprop_add_potential": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    "gbprop_finalize": (C.c_int, [C.c_void_p]),
+    "gbprop_advance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_double]),
+    "gbprop_advance_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_double]),
+    "gbprop_matvec": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
+    "gbprop_multiply_sqrt_overlap": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbprop_solve_sqrt_overlap": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "gbprop_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "gbprop_reset_stats": (C.c_int, [C.c_void_p]),
+    "gbprop_get_hessenberg": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbprop_synchronize": (C.c_int, [C.c_void_p]),
+    "gbprop_tensor_multiply_bandnh": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double,
+                                                C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+}
+
+
+def declared_symbols():
+    """Every extern "C" function name declared in include/gbprop.h."""
+    import re
+    hdr = os.path.join(os.path.dirname(_HERE), "include", "gbprop.h")
+    text = open(hdr).read()
+    return sorted(set(re.findall(r"\b(gbprop_[a-z_0-9]+)\s*\(", text)))
+
+
+def lib():
+    """Load libgbprop.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libgbprop.so not built (run pyprop_gb300/csrc/build.py or __graft_entry__.build())")
+    L = C.CDLL(LIB_PATH)
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != GBPROP_OK:
+        msg = lib().gbprop_last_error()
+        raise GbpropError(status, msg.decode() if msg else "")
+    return status
+
+
+def ptr(x):
+    """Device or host address of a torch tensor / numpy array, or None."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return C.c_void_p(x.data_ptr())
+    if hasattr(x, "ctypes"):
+        return C.c_void_p(x.ctypes.data)
+    return C.c_void_p(int(x))
+
+
+class Handle:
+    """Owning wrapper of a gbprop_handle."""
+
+    def __init__(self, nl, nr, precision=FP64, krylov_basis_size=20, exponentiation_method=0,
+                 double_orthogonalization=False, stream=None):
+        L = lib()
+        h = C.c_void_p()
+        check(L.gbprop_create(C.byref(h), int(nl), int(nr), int(precision), int(krylov_basis_size),
+                              int(exponentiation_method), int(bool(double_orthogonalization)),
+                              C.c_void_p(stream or 0)))
+        self._h = h
+        self.nl, self.nr, self.precision, self.m = nl, nr, precision, krylov_basis_size
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None) and self._h.value:
+                lib().gbprop_destroy(self._h)
+                self._h = C.c_void_p()
+        except Exception:
+            pass
+
+    @property
+    def raw(self):
+        return self._h
+
+    def set_overlap(self, kd, U_band):
+        import numpy as np
+        U = np.ascontiguousarray(U_band, dtype=np.float64)
+        check(lib().gbprop_set_overlap(self._h, int(kd), ptr(U)))
+
+    def add_potential(self, storage, pairs, kb, data, time_dependent):
+        import numpy as np
+        d = np.ascontiguousarray(data, dtype=np.complex128)
+        npairs = d.shape[0]
+        p = None
+        if pairs is not None:
+            p = np.ascontiguousarray(pairs, dtype=np.int32)
+        check(lib().gbprop_add_potential(self._h, int(storage), int(npairs), ptr(p), int(kb), ptr(d),
+                                         int(bool(time_dependent))))
+
+    def finalize(self):
+        check(lib().gbprop_finalize(self._h))
+
+    def advance(self, psi_dev, scalings, dt):
+        import numpy as np
+        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        dt = complex(dt)
+        check(lib().gbprop_advance(self._h, ptr(psi_dev), int(len(s)), ptr(s), dt.real, dt.imag))
+
+    def advance_host(self, psi_host, scalings, dt):
+        import numpy as np
+        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        dt = complex(dt)
+        check(lib().gbprop_advance_host(self._h, ptr(psi_host), int(len(s)), ptr(s), dt.real, dt.imag))
+
+    def matvec(self, src, dst, scaling, balanced=True):
+        check(lib().gbprop_matvec(self._h, ptr(src), ptr(dst), float(scaling), int(bool(balanced))))
+
+    def multiply_sqrt_overlap(self, psi):
+        check(lib().gbprop_multiply_sqrt_overlap(self._h, ptr(psi)))
+
+    def solve_sqrt_overlap(self, conj, psi):
+        check(lib().gbprop_solve_sqrt_overlap(self._h, int(bool(conj)), ptr(psi)))
+
+    def stats(self):
+        st = Stats()
+        check(lib().gbprop_get_stats(self._h, C.byref(st)))
+        return st
+
+    def reset_stats(self):
+        check(lib().gbprop_reset_stats(self._h))
+
+    def hessenberg(self):
+        import numpy as np
+        out = np.zeros((self.m, self.m), dtype=np.complex128)
+        check(lib().gbprop_get_hessenberg(self._h, ptr(out)))
+        return out
+
+    def synchronize(self):
+        check(lib().gbprop_synchronize(self._h))
+
+
+def launch_count():
+    return int(lib().gbprop_launch_count())

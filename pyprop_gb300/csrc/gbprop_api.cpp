@@ -1,0 +1,705 @@
+// Host runtime of libgbprop: the C ABI declared in include/gbprop.h.
+//
+// One handle = one propagation problem (the reference's PamPropagator +
+// krylov_PampWrapper_<2> + the consolidated TensorPotential list of its
+// BasisPropagator).  The handle owns the operator tables and the Krylov
+// workspace on the device; the wavefunction stays caller-owned, as in the
+// reference (pampwrapper.cpp:28-33 wraps the caller's buffers).  A propagation
+// step is enqueued as a fixed kernel sequence on the handle's stream and is
+// captured once into a CUDA graph, replayed per step; per-step values (time
+// function, time step) are read by the kernels from a device schedule array.
+#include "gbprop_internal.h"
+#include "../../include/gbprop.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace gbprop {
+static std::atomic<long long> g_launches{0};
+void count_launch(int n) { g_launches += n; }
+long long launch_count() { return g_launches.load(); }
+}  // namespace gbprop
+
+using namespace gbprop;
+
+namespace {
+
+thread_local std::string t_err;
+
+gbprop_status fail(gbprop_status st, const std::string& msg) {
+    t_err = msg;
+    return st;
+}
+
+#define GB_CUDA(call)                                                                                  \
+    do {                                                                                               \
+        cudaError_t _e = (call);                                                                       \
+        if (_e != cudaSuccess)                                                                         \
+            return fail(GBPROP_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e));             \
+    } while (0)
+
+struct HostPot {
+    int storage;
+    int npairs;
+    std::vector<int> pairs;
+    int kb;
+    std::vector<double> data;   // complex interleaved, (npairs, (2kb+1)*nr)
+    int timedep;
+};
+
+// Device copies of one precision's tables.
+template <typename T> struct DevTables {
+    SolveTab<T> tab[2];        // [0]: U^-1,  [1]: U^-T
+    BandOp<T> op;
+};
+
+}  // namespace
+
+struct gbprop_ctx {
+    int nl = 0, nr = 0, prec = 0, m = 0, expm_method = 0, double_orth = 0;
+    long N = 0;
+    cudaStream_t stream = nullptr;    // owned capture/work stream (non-blocking)
+    cudaStream_t ustream = nullptr;   // caller's stream; ordered against `stream` by events
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    void* d_host_stage = nullptr;     // device copy used by gbprop_advance_host
+    int kd = -1;
+    std::vector<double> U;            // upper band storage (nr, kd+1)
+    std::vector<HostPot> pots;
+    int kb = -1;
+    bool finalized = false;
+
+    DevTables<double> t64;
+    DevTables<float> t32;
+    double* d_ud_phys = nullptr;      // (kd+1) x nr : U(i, i+d)
+    Ctrl* d_ctrl = nullptr;
+    double* d_H = nullptr;
+    SchedEntry* d_sched = nullptr;
+    int sched_cap = 0;
+    double* d_partials = nullptr;
+    unsigned* d_counter = nullptr;
+    void* d_V = nullptr;              // m x N, Krylov precision
+    void* d_r = nullptr;              // N, Krylov precision (residual / w)
+    void* d_s = nullptr;              // N, Krylov precision (U^-1 v)
+    void* d_y = nullptr;              // N, Krylov precision (H U^-1 v)
+    double2* d_x = nullptr;           // N, complex128 (U psi, V y)
+    std::vector<void*> allocs;
+
+    cudaGraphExec_t graph = nullptr;
+    const void* graph_psi = nullptr;
+    long long graph_launches = 0;
+
+    ~gbprop_ctx() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : allocs) cudaFree(p);
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_out) cudaEventDestroy(ev_out);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    // order the handle's work after / before the caller's stream
+    cudaError_t begin() {
+        cudaError_t e = cudaEventRecord(ev_in, ustream);
+        if (e != cudaSuccess) return e;
+        return cudaStreamWaitEvent(stream, ev_in, 0);
+    }
+    cudaError_t end() {
+        cudaError_t e = cudaEventRecord(ev_out, stream);
+        if (e != cudaSuccess) return e;
+        return cudaStreamWaitEvent(ustream, ev_out, 0);
+    }
+
+    int kprec() const { return prec == GBPROP_FP64 ? 0 : 1; }     // 0 = complex128, 1 = complex64
+    size_t kelem() const { return prec == GBPROP_FP64 ? sizeof(double2) : sizeof(float2); }
+
+    template <typename P> gbprop_status dalloc(P** out, size_t bytes) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+        if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(p);
+        *out = (P*)p;
+        return GBPROP_OK;
+    }
+    template <typename V> gbprop_status upload(V** out, const std::vector<V>& host) {
+        gbprop_status st = dalloc(out, host.size() * sizeof(V));
+        if (st) return st;
+        cudaError_t e = cudaMemcpyAsync(*out, host.data(), host.size() * sizeof(V), cudaMemcpyHostToDevice, stream);
+        if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+        return GBPROP_OK;
+    }
+};
+
+namespace {
+
+// ---- tables of the parallel triangular solve -------------------------------
+struct HostSolveTab {
+    int n, kd, L, P, levels, dir;
+    std::vector<double> ud, invd, g, mlev;
+};
+
+// U(i, j) from upper band storage, 0 outside the band.
+double uval(const std::vector<double>& U, int n, int kd, int i, int j) {
+    if (i < 0 || j < 0 || i >= n || j >= n || j < i || j > i + kd) return 0.0;
+    return U[(size_t)j * (kd + 1) + kd + i - j];
+}
+
+// Build the tables for U x = b (dir 0) or U^T x = b (dir 1), the latter written
+// as an upper solve in reversed coordinates e = n-1-p.
+HostSolveTab build_solve_tab(const std::vector<double>& U, int n, int kd, int dir) {
+    HostSolveTab t;
+    t.n = n;
+    t.kd = kd;
+    t.dir = dir;
+    int L = (n + kSolveLanes - 1) / kSolveLanes;
+    if (L < kd) L = kd;
+    if (L < 1) L = 1;
+    t.L = L;
+    t.P = (n + L - 1) / L;
+    int lev = 0;
+    while ((1 << lev) < t.P) ++lev;
+    t.levels = lev;
+    auto ut = [&](int e, int f) -> double {       // upper matrix in e coordinates
+        if (dir == 0) return uval(U, n, kd, e, f);
+        return uval(U, n, kd, n - 1 - f, n - 1 - e);
+    };
+    t.ud.assign((size_t)std::max(kd, 1) * L * 32, 0.0);
+    t.invd.assign((size_t)L * 32, 0.0);
+    t.g.assign((size_t)std::max(kd, 1) * L * 32, 0.0);
+    t.mlev.assign((size_t)std::max(lev, 1) * 32 * kd * kd, 0.0);
+    std::vector<std::vector<double>> F(t.P, std::vector<double>((size_t)kd * kd, 0.0));
+    for (int B = 0; B < t.P; ++B) {
+        const int e0 = B * L, e1 = std::min(n, e0 + L), Lb = e1 - e0;
+        for (int i = 0; i < Lb; ++i) {
+            const int e = e0 + i;
+            const double dg = ut(e, e);
+            t.invd[(size_t)i * 32 + B] = 1.0 / dg;
+            for (int d = 1; d <= kd; ++d)
+                if (i + d < Lb) t.ud[((size_t)(d - 1) * L + i) * 32 + B] = ut(e, e + d) / dg;
+        }
+        if (B + 1 >= t.P) continue;
+        // G_B = U_BB^-1 C_B, C_B[i][c] = U~(e0+i, e1+c); back substitution per column c
+        std::vector<double> G((size_t)Lb * kd, 0.0);
+        for (int c = 0; c < kd; ++c) {
+            if (e1 + c >= n) continue;
+            for (int i = Lb - 1; i >= 0; --i) {
+                const int e = e0 + i;
+                double s = ut(e, e1 + c);
+                for (int d = 1; d <= kd && i + d < Lb; ++d) s -= ut(e, e + d) * G[(size_t)(i + d) * kd + c];
+                G[(size_t)i * kd + c] = s / ut(e, e);
+            }
+        }
+        for (int i = 0; i < Lb; ++i)
+            for (int c = 0; c < kd; ++c) t.g[((size_t)c * L + i) * 32 + B] = G[(size_t)i * kd + c];
+        for (int r = 0; r < kd && r < Lb; ++r)
+            for (int c = 0; c < kd; ++c) F[B][(size_t)r * kd + c] = -G[(size_t)r * kd + c];
+    }
+    // suffix-scan operators: M^0_B = -F_B, M^{l+1}_B = M^l_B M^l_{B+s}
+    std::vector<std::vector<double>> M = F;
+    for (int lv = 0; lv < lev; ++lv) {
+        const int s = 1 << lv;
+        for (int B = 0; B < t.P; ++B)
+            for (int k = 0; k < kd * kd; ++k) t.mlev[((size_t)(lv * 32 + B)) * kd * kd + k] = M[B][k];
+        std::vector<std::vector<double>> Mn(t.P, std::vector<double>((size_t)kd * kd, 0.0));
+        for (int B = 0; B + s < t.P; ++B)
+            for (int r = 0; r < kd; ++r)
+                for (int c = 0; c < kd; ++c) {
+                    double acc = 0.0;
+                    for (int k = 0; k < kd; ++k) acc += M[B][(size_t)r * kd + k] * M[B + s][(size_t)k * kd + c];
+                    Mn[B][(size_t)r * kd + c] = acc;
+                }
+        M.swap(Mn);
+    }
+    return t;
+}
+
+template <typename T>
+gbprop_status upload_solve_tab(gbprop_ctx* h, const HostSolveTab& ht, SolveTab<T>* out) {
+    auto cvt = [](const std::vector<double>& v) { return std::vector<T>(v.begin(), v.end()); };
+    T *ud, *invd, *g, *ml;
+    gbprop_status st;
+    if ((st = h->upload(&ud, cvt(ht.ud)))) return st;
+    if ((st = h->upload(&invd, cvt(ht.invd)))) return st;
+    if ((st = h->upload(&g, cvt(ht.g)))) return st;
+    if ((st = h->upload(&ml, cvt(ht.mlev)))) return st;
+    out->n = ht.n;
+    out->kd = ht.kd;
+    out->L = ht.L;
+    out->P = ht.P;
+    out->levels = ht.levels;
+    out->dir = ht.dir;
+    out->ud = ud;
+    out->invd = invd;
+    out->g = g;
+    out->mlev = ml;
+    return GBPROP_OK;
+}
+
+// ---- term list of the tensor-potential matvec -------------------------------
+struct HostBandOp {
+    int kb;
+    std::vector<int> row_ptr, src, slot, timedep;
+    std::vector<double> coef;
+    std::vector<double> slots;   // nslots x (2kb+1) x nr
+};
+
+HostBandOp build_band_op(const gbprop_ctx* h) {
+    HostBandOp op;
+    op.kb = h->kb;
+    const int nr = h->nr, kb = h->kb, W = 2 * kb + 1;
+    struct Term { int dst, src, slot, td; double cr, ci; };
+    std::vector<Term> terms;
+    int nslots = 0;
+    for (const HostPot& p : h->pots) {
+        // split complex band data into a real part (coefficient 1) and an
+        // imaginary part (coefficient i); a part that is identically zero is dropped
+        for (int part = 0; part < 2; ++part) {
+            bool any = false;
+            for (size_t k = part; k < p.data.size(); k += 2)
+                if (p.data[k] != 0.0) { any = true; break; }
+            if (!any) continue;
+            const double cr = part == 0 ? 1.0 : 0.0, ci = part == 0 ? 0.0 : 1.0;
+            for (int q = 0; q < p.npairs; ++q) {
+                const int slot = nslots++;
+                op.slots.resize((size_t)nslots * W * nr, 0.0);
+                double* S = op.slots.data() + (size_t)slot * W * nr;
+                const double* D = p.data.data() + (size_t)q * W * nr * 2;
+                for (int i = 0; i < nr; ++i)
+                    for (int d = 0; d < W; ++d) {
+                        const int j = i + d - kb;
+                        if (j < 0 || j >= nr) continue;
+                        S[(size_t)d * nr + i] = D[2 * ((size_t)j * W + kb + i - j) + part];
+                    }
+                if (p.storage == GBPROP_STORAGE_DIAG) {
+                    terms.push_back({q, q, slot, p.timedep, cr, ci});
+                } else if (p.storage == GBPROP_STORAGE_IDENT) {
+                    for (int l = 0; l < h->nl; ++l) terms.push_back({l, l, slot, p.timedep, cr, ci});
+                } else {
+                    terms.push_back({p.pairs[2 * q], p.pairs[2 * q + 1], slot, p.timedep, cr, ci});
+                }
+            }
+        }
+    }
+    std::stable_sort(terms.begin(), terms.end(), [](const Term& a, const Term& b) { return a.dst < b.dst; });
+    op.row_ptr.assign(h->nl + 1, 0);
+    for (const Term& t : terms) {
+        op.row_ptr[t.dst + 1]++;
+        op.src.push_back(t.src);
+        op.slot.push_back(t.slot);
+        op.timedep.push_back(t.td);
+        op.coef.push_back(t.cr);
+        op.coef.push_back(t.ci);
+    }
+    for (int l = 0; l < h->nl; ++l) op.row_ptr[l + 1] += op.row_ptr[l];
+    return op;
+}
+
+template <typename T>
+gbprop_status upload_band_op(gbprop_ctx* h, const HostBandOp& ho, BandOp<T>* out) {
+    int *rp, *src, *slot, *td;
+    double* coef;
+    T* slots;
+    gbprop_status st;
+    std::vector<int> srcv = ho.src.empty() ? std::vector<int>{0} : ho.src;
+    std::vector<int> slotv = ho.slot.empty() ? std::vector<int>{0} : ho.slot;
+    std::vector<int> tdv = ho.timedep.empty() ? std::vector<int>{0} : ho.timedep;
+    std::vector<double> coefv = ho.coef.empty() ? std::vector<double>{0, 0} : ho.coef;
+    std::vector<T> sl(ho.slots.begin(), ho.slots.end());
+    if (sl.empty()) sl.push_back(0);
+    if ((st = h->upload(&rp, ho.row_ptr))) return st;
+    if ((st = h->upload(&src, srcv))) return st;
+    if ((st = h->upload(&slot, slotv))) return st;
+    if ((st = h->upload(&td, tdv))) return st;
+    if ((st = h->upload(&coef, coefv))) return st;
+    if ((st = h->upload(&slots, sl))) return st;
+    out->nl = h->nl;
+    out->nr = h->nr;
+    out->kb = ho.kb;
+    out->nterms = (int)ho.src.size();
+    out->row_ptr = rp;
+    out->t_src = src;
+    out->t_slot = slot;
+    out->t_timedep = td;
+    out->t_coef = coef;
+    out->slots = slots;
+    return GBPROP_OK;
+}
+
+gbprop_status check_handle(gbprop_handle h, bool need_final) {
+    if (!h) return fail(GBPROP_EINVAL, "null handle");
+    if (need_final && !h->finalized) return fail(GBPROP_EINVAL, "handle not finalized (call gbprop_finalize)");
+    return GBPROP_OK;
+}
+
+#define GB_LAUNCH(call)                                                                            \
+    do {                                                                                           \
+        cudaError_t _e = (call);                                                                   \
+        if (_e != cudaSuccess) return fail(GBPROP_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+const void* ktab(gbprop_ctx* h, int which) {
+    return h->prec == GBPROP_FP64 ? (const void*)&h->t64.tab[which] : (const void*)&h->t32.tab[which];
+}
+const void* kop(gbprop_ctx* h) {
+    return h->prec == GBPROP_FP64 ? (const void*)&h->t64.op : (const void*)&h->t32.op;
+}
+
+// Enqueue one AdvanceStep (PamPropagator.py:50-57 around pamp.h:613-669).
+gbprop_status enqueue_step(gbprop_ctx* h, void* psi) {
+    cudaStream_t s = h->stream;
+    const int kp = h->kprec();
+    const int m = h->m;
+    const long N = h->N;
+    char* V = (char*)h->d_V;
+    const size_t vbytes = (size_t)N * h->kelem();
+    GB_LAUNCH(launch_step_begin(h->d_ctrl, h->d_H, m, s));
+    // psi <- U psi (MultiplySqrtOverlap(false)), kept in complex128, and beta0 = ||U psi||
+    GB_LAUNCH(launch_tbmv(0, h->kd, h->d_ud_phys, h->nl, h->nr, psi, kp, h->d_x, 0, s));
+    GB_LAUNCH(launch_norm(0, h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
+    for (int J = 0; J < m; ++J) {
+        const void* in = J == 0 ? (const void*)h->d_x : (const void*)h->d_r;
+        const int in_prec = J == 0 ? 0 : kp;
+        // v_J = r / beta_J stored in V[J]; s = U^-1 v_J
+        GB_LAUNCH(launch_solve(kp, ktab(h, 0), h->nl, in, in_prec, h->d_s, kp, V + J * vbytes, kp, h->d_ctrl, 1, 1, s));
+        // y = sum_t c_t s_t A_t s
+        GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, h->d_sched, h->d_ctrl, 0.0, 1, s));
+        // w = U^-T y
+        GB_LAUNCH(launch_solve(kp, ktab(h, 1), h->nl, h->d_y, kp, h->d_r, kp, nullptr, kp, h->d_ctrl, 0, 1, s));
+        // classical Gram-Schmidt against v_0..v_J
+        GB_LAUNCH(launch_cgs_dot(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0, h->double_orth, s));
+        if (J < m - 1 || h->double_orth)
+            GB_LAUNCH(launch_cgs_update(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl,
+                                        h->double_orth ? 2 : 0, s));
+        if (h->double_orth) {
+            for (int pass = 0; pass < 3; ++pass) {
+                GB_LAUNCH(launch_cgs_dot(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, 0, s));
+                GB_LAUNCH(launch_cgs_update(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, s));
+            }
+        }
+        GB_LAUNCH(launch_arnoldi_finalize(h->d_ctrl, h->d_H, m, J, h->double_orth, s));
+    }
+    GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, s));
+    GB_LAUNCH(launch_combine(kp, V, N, h->d_ctrl, h->d_x, s));
+    // psi <- U^-1 (beta0 V y)  (SolveSqrtOverlap(false))
+    GB_LAUNCH(launch_solve(0, &h->t64.tab[0], h->nl, h->d_x, 0, psi, kp, nullptr, 0, h->d_ctrl, 0, 0, s));
+    GB_LAUNCH(launch_step_end(h->d_ctrl, s));
+    return GBPROP_OK;
+}
+
+gbprop_status ensure_graph(gbprop_ctx* h, void* psi) {
+    if (h->graph && h->graph_psi == psi) return GBPROP_OK;
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    GB_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = launch_count();
+    gbprop_status st = enqueue_step(h, psi);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (st) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    h->graph_launches = launch_count() - before;
+    // the captured launches did not run; take them off the process counter
+    count_launch((int)-h->graph_launches);
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    h->graph_psi = psi;
+    return GBPROP_OK;
+}
+
+gbprop_status ensure_sched(gbprop_ctx* h, int n) {
+    if (n <= h->sched_cap) return GBPROP_OK;
+    // the schedule pointer is baked into the graph: grow by re-allocation and re-capture
+    int cap = std::max(n, std::max(1024, 2 * h->sched_cap));
+    SchedEntry* p = nullptr;
+    GB_CUDA(cudaStreamSynchronize(h->stream));
+    gbprop_status st = h->dalloc(&p, (size_t)cap * sizeof(SchedEntry));
+    if (st) return st;
+    h->d_sched = p;
+    h->sched_cap = cap;
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+        h->graph_psi = nullptr;
+    }
+    return GBPROP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbprop_version(void) { return "gbprop 0.1 (sm_103a)"; }
+const char* gbprop_last_error(void) { return t_err.c_str(); }
+long long gbprop_launch_count(void) { return launch_count(); }
+
+gbprop_status gbprop_create(gbprop_handle* out, int nl, int nr, int precision, int krylov_basis_size,
+                            int exponentiation_method, int double_orthogonalization, void* stream) {
+    if (!out) return fail(GBPROP_EINVAL, "null output pointer");
+    *out = nullptr;
+    if (nl <= 0 || nr <= 0) return fail(GBPROP_EINVAL, "nl and nr must be positive");
+    if (precision != GBPROP_FP64 && precision != GBPROP_FP32_MIXED) return fail(GBPROP_EINVAL, "unknown precision");
+    if (krylov_basis_size < 1 || krylov_basis_size > kMaxBasis)
+        return fail(GBPROP_EINVAL, "krylov_basis_size must be in [1, 64]");
+    if (exponentiation_method != 0)
+        return fail(GBPROP_EUNSUPPORTED, "krylov_exponentiation_method=1 (eigenvector) is not provided; use 0 (Pade)");
+    gbprop_ctx* h = new gbprop_ctx();
+    h->nl = nl;
+    h->nr = nr;
+    h->N = (long)nl * nr;
+    h->prec = precision;
+    h->m = krylov_basis_size;
+    h->expm_method = exponentiation_method;
+    h->double_orth = double_orthogonalization ? 1 : 0;
+    h->ustream = (cudaStream_t)stream;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(GBPROP_ECUDA, std::string("stream/event creation: ") + cudaGetErrorString(e));
+    }
+    *out = h;
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_destroy(gbprop_handle h) {
+    if (!h) return GBPROP_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    delete h;
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_set_overlap(gbprop_handle h, int kd, const double* U_band) {
+    if (gbprop_status st = check_handle(h, false)) return st;
+    if (h->finalized) return fail(GBPROP_EINVAL, "handle already finalized");
+    if (kd < 1 || kd > kMaxKd) return fail(GBPROP_EUNSUPPORTED, "overlap band half-width must be in [1, 8]");
+    if (!U_band) return fail(GBPROP_EINVAL, "null overlap factor");
+    if (h->nr < kd + 1) return fail(GBPROP_EINVAL, "radial size smaller than the overlap band");
+    h->kd = kd;
+    h->U.assign(U_band, U_band + (size_t)h->nr * (kd + 1));
+    for (int i = 0; i < h->nr; ++i)
+        if (!(uval(h->U, h->nr, kd, i, i) != 0.0)) return fail(GBPROP_EINVAL, "zero on the overlap factor diagonal");
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_add_potential(gbprop_handle h, int storage, int npairs, const int* pairs, int kb,
+                                   const double* data, int time_dependent) {
+    if (gbprop_status st = check_handle(h, false)) return st;
+    if (h->finalized) return fail(GBPROP_EINVAL, "handle already finalized");
+    if (storage != GBPROP_STORAGE_DIAG && storage != GBPROP_STORAGE_IDENT && storage != GBPROP_STORAGE_SIMP)
+        return fail(GBPROP_EUNSUPPORTED, "angular storage must be Diag, Ident or Simp");
+    if (kb < 0 || 2 * kb + 1 > 2 * h->nr + 1) return fail(GBPROP_EINVAL, "bad band half-width");
+    if (h->kb >= 0 && kb != h->kb) return fail(GBPROP_EUNSUPPORTED, "all potentials must share one radial band width");
+    if (!data) return fail(GBPROP_EINVAL, "null potential data");
+    if (storage == GBPROP_STORAGE_DIAG && npairs != h->nl) return fail(GBPROP_EINVAL, "Diag storage needs npairs == nl");
+    if (storage == GBPROP_STORAGE_IDENT && npairs != 1) return fail(GBPROP_EINVAL, "Ident storage needs npairs == 1");
+    if (storage == GBPROP_STORAGE_SIMP) {
+        if (!pairs || npairs < 0) return fail(GBPROP_EINVAL, "Simp storage needs a pair table");
+        for (int q = 0; q < npairs; ++q)
+            if (pairs[2 * q] < 0 || pairs[2 * q] >= h->nl || pairs[2 * q + 1] < 0 || pairs[2 * q + 1] >= h->nl)
+                return fail(GBPROP_EINVAL, "angular pair index out of range");
+    }
+    HostPot p;
+    p.storage = storage;
+    p.npairs = npairs;
+    if (storage == GBPROP_STORAGE_SIMP) p.pairs.assign(pairs, pairs + 2 * (size_t)npairs);
+    p.kb = kb;
+    p.data.assign(data, data + (size_t)npairs * (2 * kb + 1) * h->nr * 2);
+    p.timedep = time_dependent ? 1 : 0;
+    h->kb = kb;
+    h->pots.push_back(std::move(p));
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_finalize(gbprop_handle h) {
+    if (gbprop_status st = check_handle(h, false)) return st;
+    if (h->finalized) return GBPROP_OK;
+    if (h->kd < 0) return fail(GBPROP_EINVAL, "overlap factor not set");
+    if (h->kb < 0) h->kb = h->kd;
+    gbprop_status st;
+    // solve tables: FP64 always (state transforms), FP32 for the mixed Krylov basis
+    for (int dir = 0; dir < 2; ++dir) {
+        HostSolveTab ht = build_solve_tab(h->U, h->nr, h->kd, dir);
+        if ((st = upload_solve_tab<double>(h, ht, &h->t64.tab[dir]))) return st;
+        if (h->prec == GBPROP_FP32_MIXED)
+            if ((st = upload_solve_tab<float>(h, ht, &h->t32.tab[dir]))) return st;
+    }
+    HostBandOp ho = build_band_op(h);
+    if (h->prec == GBPROP_FP64) {
+        if ((st = upload_band_op<double>(h, ho, &h->t64.op))) return st;
+    } else {
+        if ((st = upload_band_op<float>(h, ho, &h->t32.op))) return st;
+    }
+    std::vector<double> udp((size_t)(h->kd + 1) * h->nr, 0.0);
+    for (int d = 0; d <= h->kd; ++d)
+        for (int i = 0; i + d < h->nr; ++i) udp[(size_t)d * h->nr + i] = uval(h->U, h->nr, h->kd, i, i + d);
+    if ((st = h->upload(&h->d_ud_phys, udp))) return st;
+    if ((st = h->dalloc(&h->d_ctrl, sizeof(Ctrl)))) return st;
+    GB_CUDA(cudaMemsetAsync(h->d_ctrl, 0, sizeof(Ctrl), h->stream));
+    if ((st = h->dalloc(&h->d_H, (size_t)2 * h->m * h->m * sizeof(double)))) return st;
+    GB_CUDA(cudaMemsetAsync(h->d_H, 0, (size_t)2 * h->m * h->m * sizeof(double), h->stream));
+    if ((st = h->dalloc(&h->d_partials, (size_t)grid_reduce_blocks() * (2 * kMaxBasis + 4) * sizeof(double)))) return st;
+    if ((st = h->dalloc(&h->d_counter, 64))) return st;
+    GB_CUDA(cudaMemsetAsync(h->d_counter, 0, 64, h->stream));
+    const size_t ke = h->kelem();
+    if ((st = h->dalloc(&h->d_V, (size_t)h->m * h->N * ke))) return st;
+    GB_CUDA(cudaMemsetAsync(h->d_V, 0, (size_t)h->m * h->N * ke, h->stream));
+    if ((st = h->dalloc(&h->d_r, (size_t)h->N * ke))) return st;
+    if ((st = h->dalloc(&h->d_s, (size_t)h->N * ke))) return st;
+    if ((st = h->dalloc(&h->d_y, (size_t)h->N * ke))) return st;
+    if ((st = h->dalloc(&h->d_x, (size_t)h->N * sizeof(double2)))) return st;
+    if ((st = ensure_sched(h, 1024))) return st;
+    GB_CUDA(cudaStreamSynchronize(h->stream));
+    h->finalized = true;
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_advance(gbprop_handle h, void* psi, int nsteps, const double* scalings, double dt_re,
+                             double dt_im) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!psi) return fail(GBPROP_EINVAL, "null wavefunction");
+    if (nsteps < 0) return fail(GBPROP_EINVAL, "negative step count");
+    if (nsteps == 0) return GBPROP_OK;
+    if (!scalings) return fail(GBPROP_EINVAL, "null scaling schedule");
+    gbprop_status st;
+    GB_CUDA(h->begin());
+    // steps are issued in chunks of the schedule capacity
+    int done = 0;
+    while (done < nsteps) {
+        const int chunk = std::min(nsteps - done, std::max(h->sched_cap, 1024));
+        if ((st = ensure_sched(h, chunk))) return st;
+        std::vector<SchedEntry> sched(chunk);
+        for (int k = 0; k < chunk; ++k) sched[k] = {scalings[done + k], dt_re, dt_im};
+        // pageable source: staged before the call returns, so `sched` may go out of scope
+        GB_CUDA(cudaMemcpyAsync(h->d_sched, sched.data(), chunk * sizeof(SchedEntry), cudaMemcpyHostToDevice, h->stream));
+        GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), h->stream));
+        if ((st = ensure_graph(h, psi))) return st;
+        for (int k = 0; k < chunk; ++k) {
+            GB_CUDA(cudaGraphLaunch(h->graph, h->stream));
+            count_launch((int)h->graph_launches);
+        }
+        done += chunk;
+    }
+    GB_CUDA(h->end());
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_advance_host(gbprop_handle h, void* psi_host, int nsteps, const double* scalings, double dt_re,
+                                  double dt_im) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!psi_host) return fail(GBPROP_EINVAL, "null wavefunction");
+    const size_t bytes = (size_t)h->N * (h->prec == GBPROP_FP64 ? sizeof(double2) : sizeof(float2));
+    if (!h->d_host_stage) {
+        gbprop_status st = h->dalloc(&h->d_host_stage, bytes);
+        if (st) return st;
+    }
+    void* d = h->d_host_stage;
+    GB_CUDA(cudaMemcpyAsync(d, psi_host, bytes, cudaMemcpyHostToDevice, h->ustream));
+    gbprop_status st = gbprop_advance(h, d, nsteps, scalings, dt_re, dt_im);
+    if (st) return st;
+    GB_CUDA(cudaMemcpyAsync(psi_host, d, bytes, cudaMemcpyDeviceToHost, h->ustream));
+    GB_CUDA(cudaStreamSynchronize(h->ustream));
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_matvec(gbprop_handle h, const void* src, void* dst, double scaling, int balanced) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!src || !dst) return fail(GBPROP_EINVAL, "null vector");
+    if (src == dst) return fail(GBPROP_EINVAL, "src and dst must differ");
+    const int kp = h->kprec();
+    cudaStream_t s = h->stream;
+    GB_CUDA(h->begin());
+    if (balanced) {
+        GB_LAUNCH(launch_solve(kp, ktab(h, 0), h->nl, src, kp, h->d_s, kp, nullptr, kp, h->d_ctrl, 0, 0, s));
+        GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, nullptr, h->d_ctrl, scaling, 0, s));
+        GB_LAUNCH(launch_solve(kp, ktab(h, 1), h->nl, h->d_y, kp, dst, kp, nullptr, kp, h->d_ctrl, 0, 0, s));
+    } else {
+        GB_LAUNCH(launch_band_apply(kp, kop(h), src, dst, nullptr, h->d_ctrl, scaling, 0, s));
+    }
+    GB_CUDA(h->end());
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_multiply_sqrt_overlap(gbprop_handle h, void* psi) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!psi) return fail(GBPROP_EINVAL, "null wavefunction");
+    const int kp = h->kprec();
+    GB_CUDA(h->begin());
+    GB_LAUNCH(launch_tbmv(0, h->kd, h->d_ud_phys, h->nl, h->nr, psi, kp, h->d_r, kp, h->stream));
+    GB_CUDA(cudaMemcpyAsync(psi, h->d_r, (size_t)h->N * h->kelem(), cudaMemcpyDeviceToDevice, h->stream));
+    GB_CUDA(h->end());
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_solve_sqrt_overlap(gbprop_handle h, int conj, void* psi) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!psi) return fail(GBPROP_EINVAL, "null wavefunction");
+    const int kp = h->kprec();
+    GB_CUDA(h->begin());
+    GB_LAUNCH(launch_solve(0, &h->t64.tab[conj ? 1 : 0], h->nl, psi, kp, psi, kp, nullptr, 0, h->d_ctrl, 0, 0, h->stream));
+    GB_CUDA(h->end());
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_get_stats(gbprop_handle h, gbprop_stats* out) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!out) return fail(GBPROP_EINVAL, "null output");
+    Ctrl c;
+    GB_CUDA(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA(cudaStreamSynchronize(h->stream));
+    out->operator_count = c.operator_count;
+    out->inner_product_count = c.inner_product_count;
+    out->orthogonalization_count = c.orthogonalization_count;
+    out->breakdown_count = c.breakdown_count;
+    out->step_count = c.step_count;
+    out->last_basis_size = c.nbasis;
+    out->last_scaling_order = c.scaling_order;
+    out->error_estimate = c.err_est;
+    if (c.lu_info) return fail(GBPROP_ELU, "Pade denominator singular (LU info " + std::to_string(c.lu_info) + ")");
+    if (c.nonfinite) return fail(GBPROP_ENONFINITE, "non-finite Krylov norm");
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_reset_stats(gbprop_handle h) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    GB_CUDA(cudaMemsetAsync(h->d_ctrl, 0, sizeof(Ctrl), h->stream));
+    GB_CUDA(cudaStreamSynchronize(h->stream));
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_get_hessenberg(gbprop_handle h, double* out) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!out) return fail(GBPROP_EINVAL, "null output");
+    GB_CUDA(cudaMemcpyAsync(out, h->d_H, (size_t)2 * h->m * h->m * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA(cudaStreamSynchronize(h->stream));
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_synchronize(gbprop_handle h) {
+    if (gbprop_status st = check_handle(h, false)) return st;
+    GB_CUDA(cudaStreamSynchronize(h->stream));
+    GB_CUDA(cudaStreamSynchronize(h->ustream));
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_tensor_multiply_bandnh(int storage, const void* V, int npairs, const int* pairs, int kb,
+                                            double scaling, const void* src, void* dst, int nl, int nr, void* stream) {
+    if (storage != GBPROP_STORAGE_DIAG && storage != GBPROP_STORAGE_SIMP)
+        return fail(GBPROP_EUNSUPPORTED, "stateless multiply supports Diag and Simp angular storage");
+    if (!V || !src || !dst) return fail(GBPROP_EINVAL, "null buffer");
+    if (storage == GBPROP_STORAGE_SIMP && (!pairs || npairs < 0)) return fail(GBPROP_EINVAL, "Simp needs pairs");
+    if (nl <= 0 || nr <= 0 || kb < 0) return fail(GBPROP_EINVAL, "bad sizes");
+    GB_LAUNCH(launch_tensor_multiply_ref(storage == GBPROP_STORAGE_DIAG ? 0 : 1, (const double2*)V, npairs, pairs, kb,
+                                         scaling, (const double2*)src, (double2*)dst, nl, nr, (cudaStream_t)stream));
+    return GBPROP_OK;
+}
+
+}  // extern "C"

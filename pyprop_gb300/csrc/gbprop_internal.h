@@ -1,0 +1,118 @@
+// Internal declarations shared by the host runtime (gbprop_api.cpp) and the
+// CUDA kernels (gbprop_kernels.cu).  Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace gbprop {
+
+constexpr int kMaxBasis = 64;       // largest krylov_basis_size a handle accepts
+constexpr int kWarp = 32;
+constexpr int kSolveLanes = 32;     // radial blocks per l-row in the parallel solve
+constexpr int kMaxKd = 8;           // largest band half-width of the overlap factor (order 9)
+
+template <typename T> struct cx_of;
+template <> struct cx_of<double> { using type = double2; };
+template <> struct cx_of<float> { using type = float2; };
+template <typename T> using cx = typename cx_of<T>::type;
+
+// Tables of the parallel upper-band triangular solve U x = b in "e" coordinates
+// (e = p for U^-1, e = n-1-p for U^-T), block-interleaved so that lane B of a
+// warp reads entry (.., i, B) coalesced.  Built on the host in FP64.
+//   n       radial length,  kd  superdiagonals,  L  block length,  P  blocks (<= 32)
+//   ud      ((d-1)*L + i)*32 + B : U(e, e+d) / U(e, e), d = 1..kd, zero outside the block
+//   invd    i*32 + B             : 1 / U(e, e), zero for e >= n
+//   g       (c*L + i)*32 + B     : coupling of x_e to x_{(B+1)L + c} (within-block solve of
+//                                  the block's upper-right corner), zero for the last block
+//   mlev    ((lev*32 + B)*kd + r)*kd + c : suffix-scan operators of the kd-vector recurrence
+//                                  t_B = y_B[0:kd] - F_B t_{B+1}, lev = 0..levels-1
+template <typename T> struct SolveTab {
+    int n, kd, L, P, levels, dir;
+    const T* ud;
+    const T* invd;
+    const T* g;
+    const T* mlev;
+};
+
+// Term list of the tensor-potential matvec, grouped by destination row l:
+//   y[l][i] += coef_t * s_t * sum_d slot[t][d][i] * x[src_t][i + d - kb]
+// slots are real bands stored diagonal-major: (slot*(2kb+1) + d)*nr + i = A(i, i+d-kb).
+template <typename T> struct BandOp {
+    int nl, nr, kb, nterms;
+    const int* row_ptr;      // nl + 1
+    const int* t_src;        // nterms
+    const int* t_slot;       // nterms
+    const int* t_timedep;    // nterms
+    const double* t_coef;    // 2 * nterms (re, im)
+    const T* slots;
+};
+
+// Device control block of one handle; every field is written by kernels only.
+struct Ctrl {
+    int step;               // index of the current entry of the schedule array
+    int broken;             // happy breakdown seen in the current step
+    int nbasis;             // Krylov vectors built in the current step
+    int lu_info;            // last non-zero LU info of the Pade solve
+    int scaling_order;      // s of the last scaling-and-squaring
+    int nonfinite;          // a NaN/Inf norm was seen
+    int ro_go;              // re-orthogonalisation requested for the current vector
+    int ro_count;           // re-orthogonalisation passes done for the current vector
+    long long operator_count;
+    long long inner_product_count;
+    long long orthogonalization_count;
+    long long breakdown_count;
+    long long step_count;
+    double beta0;           // ||U psi|| at the start of the step
+    double beta;            // current residual norm
+    double inv_beta;        // 1 / beta (the reference scales by the reciprocal)
+    double orig_norm;       // ||w|| before Gram-Schmidt (re-orthogonalisation rule)
+    double resid_norm;      // ||w|| after Gram-Schmidt
+    double err_est;         // |y[m-1]|^2
+    double h[2 * kMaxBasis];
+    double h3[2 * kMaxBasis];
+    double y[2 * kMaxBasis];
+};
+
+// Schedule entry per step: time-function value and complex time step.
+struct SchedEntry {
+    double scaling;
+    double dt_re;
+    double dt_im;
+};
+
+// Launch counter shared by all launchers (process-wide).
+void count_launch(int n = 1);
+long long launch_count();
+
+// ---- launchers (gbprop_kernels.cu) -------------------------------------------
+// All return the cudaGetLastError() of their launch.
+// Parallel banded triangular solve, one warp per l-row.
+//   in_prec/out_prec/v_prec: 0 = complex128, 1 = complex64;  arith: 0 = double, 1 = float
+//   scale_mode 1 multiplies the input by ctrl->inv_beta; vstore (if not null) receives the
+//   scaled input; check_broken skips the launch body after a happy breakdown.
+cudaError_t launch_solve(int arith, const void* tab, int nrows, const void* in, int in_prec,
+                         void* out, int out_prec, void* vstore, int v_prec, const Ctrl* ctrl,
+                         int scale_mode, int check_broken, cudaStream_t s);
+cudaError_t launch_band_apply(int arith, const void* op, const void* x, void* y, const SchedEntry* sched,
+                              const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s);
+cudaError_t launch_tbmv(int arith, int kd, const void* ud_phys, int nl, int nr, const void* in, int in_prec,
+                        void* out, int out_prec, cudaStream_t s);
+cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsigned* counter, Ctrl* ctrl,
+                        cudaStream_t s);
+cudaError_t launch_cgs_dot(int prec, const void* V, long n, int nv, const void* w, double* partials,
+                           unsigned* counter, Ctrl* ctrl, int mode, int want_norm, cudaStream_t s);
+cudaError_t launch_cgs_update(int prec, const void* V, long n, int nv, void* w, double* partials,
+                              unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
+cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, cudaStream_t s);
+cudaError_t launch_step_begin(Ctrl* ctrl, double* H, int m, cudaStream_t s);
+cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s);
+cudaError_t launch_combine(int prec, const void* V, long n, const Ctrl* ctrl, void* out, cudaStream_t s);
+cudaError_t launch_step_end(Ctrl* ctrl, cudaStream_t s);
+cudaError_t launch_tensor_multiply_ref(int storage, const double2* V, int npairs, const int* pairs, int kb,
+                                       double scaling, const double2* src, double2* dst, int nl, int nr,
+                                       cudaStream_t s);
+cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s);
+
+int grid_reduce_blocks();
+
+}  // namespace gbprop

@@ -1,0 +1,930 @@
+// CUDA kernels of the pAMP x TensorPotential propagation step, written for
+// sm_103a (GB300).  On this part FP64 issue rate is ~1/58 of FP32 and a
+// dependent FP64 FMA costs ~64 cycles, so the kernels are shaped to keep FP64
+// work minimal and never put a long FP64 dependency chain on the critical path:
+//   * the banded triangular solves along r (ztbsv in the reference) are block
+//     back-substitutions of length L with the inter-block coupling resolved by
+//     a warp-shuffle suffix scan (precomputed coupling tables), one warp per
+//     angular row;
+//   * the tensor-potential matvec applies real band slots to complex vectors
+//     (2 FMA per band entry instead of 4) with the source halo tile in smem;
+//   * Gram-Schmidt reductions are two-level (block partials + last-block
+//     finalize in fixed order: deterministic, no atomics on values).
+#include "gbprop_internal.h"
+
+#include <cfloat>
+#include <cmath>
+
+namespace gbprop {
+
+// ---------------------------------------------------------------------------
+// small complex helpers
+// ---------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ cx<T> mk(T re, T im);
+template <> __device__ __forceinline__ double2 mk<double>(double re, double im) { return make_double2(re, im); }
+template <> __device__ __forceinline__ float2 mk<float>(float re, float im) { return make_float2(re, im); }
+
+template <typename C> struct elem_of;
+template <> struct elem_of<double2> { using type = double; };
+template <> struct elem_of<float2> { using type = float; };
+
+template <typename CO, typename CI> __device__ __forceinline__ CO conv(CI v) {
+    using E = typename elem_of<CO>::type;
+    CO o;
+    o.x = (E)v.x;
+    o.y = (E)v.y;
+    return o;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Last-block detection for a two-level reduction: every block writes its
+// partials, fences, and bumps `counter`; the block that sees gridDim-1 does
+// the final sum (and resets the counter for the next launch).
+__device__ __forceinline__ bool is_last_block(unsigned* counter) {
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned v = atomicAdd(counter, 1u);
+        s_last = (v == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last != 0;
+}
+
+// Sum `nvals` values over all blocks' partials (stride `pstride` doubles per
+// block) in fixed order; result into out[0..nvals).  Called by the last block.
+__device__ void final_sum(const double* partials, int nblocks, int pstride, int nvals, double* out) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int v = warp; v < nvals; v += nw) {
+        double a = 0.0;
+        for (int b = lane; b < nblocks; b += 32) a += __ldcg(partials + (size_t)b * pstride + v);
+        a = warp_sum(a);
+        if (lane == 0) out[v] = a;
+    }
+    __syncthreads();
+}
+
+// Block-level sum of NV per-thread values into partials[blockIdx.x*pstride + off + k].
+template <int NV>
+__device__ void block_partials(double (&acc)[NV], int nvalid, double* partials, int pstride, int off) {
+    __shared__ double red[8][NV];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double v = warp_sum(acc[k]);
+        if (lane == 0) red[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV && threadIdx.x < nvalid) {
+        double s = 0.0;
+        for (int w = 0; w < nw; ++w) s += red[w][threadIdx.x];
+        partials[(size_t)blockIdx.x * pstride + off + threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// parallel banded triangular solve (ztbsv 'U','N' / 'U','C' along r)
+// ---------------------------------------------------------------------------
+constexpr int kPitch = 33;   // smem pitch of the block-interleaved row buffer
+
+template <typename T, int KD, typename TI, typename TO, typename TV>
+__global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO* out,
+                                              TV* __restrict__ vstore, const Ctrl* __restrict__ ctrl,
+                                              int scale_mode, int check_broken) {
+    using C = cx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* buf = reinterpret_cast<C*>(smem_raw);
+    if (check_broken && ctrl->broken) return;
+    const int l = blockIdx.x, lane = threadIdx.x;
+    const int n = tab.n, L = tab.L, P = tab.P;
+    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
+    const size_t base = (size_t)l * n;
+
+    for (int p = lane; p < n; p += 32) {
+        TI v = in[base + p];
+        double re = (double)v.x, im = (double)v.y;
+        if (scale_mode) { re *= sc; im *= sc; }
+        C c = mk<T>((T)re, (T)im);
+        if (vstore) vstore[base + p] = conv<TV>(c);
+        const int e = tab.dir ? (n - 1 - p) : p;
+        const int B = e / L, i = e - B * L;
+        buf[i * kPitch + B] = c;
+    }
+    __syncwarp();
+
+    // 1) local back-substitution of block B = lane (rows pre-scaled by 1/U(e,e))
+    const int B = lane;
+    C win[KD];
+#pragma unroll
+    for (int d = 0; d < KD; ++d) win[d] = mk<T>(0, 0);
+    for (int i = L - 1; i >= 0; --i) {
+        const int e = B * L + i;
+        const int idx = i * kPitch + B;
+        const T inv = tab.invd[i * 32 + B];
+        C x = mk<T>(0, 0);
+        if (e < n) {
+            const C b = buf[idx];
+            T sr = b.x * inv, si = b.y * inv;
+#pragma unroll
+            for (int d = KD; d >= 1; --d) {
+                const T u = tab.ud[((d - 1) * L + i) * 32 + B];
+                sr = fma(-u, win[d - 1].x, sr);
+                si = fma(-u, win[d - 1].y, si);
+            }
+            x = mk<T>(sr, si);
+            buf[idx] = x;
+        }
+#pragma unroll
+        for (int d = KD - 1; d >= 1; --d) win[d] = win[d - 1];
+        win[0] = x;
+    }
+
+    // 2) suffix scan of the kd-vector recurrence t_B = y_B[0:kd] - F_B t_{B+1}
+    C a[KD];
+#pragma unroll
+    for (int c = 0; c < KD; ++c) a[c] = (B * L + c < n && B < P) ? buf[c * kPitch + B] : mk<T>(0, 0);
+    for (int lev = 0; lev < tab.levels; ++lev) {
+        const int s = 1 << lev;
+        C nb[KD];
+#pragma unroll
+        for (int c = 0; c < KD; ++c) {
+            nb[c].x = __shfl_down_sync(0xffffffffu, a[c].x, s);
+            nb[c].y = __shfl_down_sync(0xffffffffu, a[c].y, s);
+        }
+        if (B + s < P) {
+            const T* M = tab.mlev + ((size_t)(lev * 32 + B) * KD) * KD;
+#pragma unroll
+            for (int r = 0; r < KD; ++r) {
+                T ar = a[r].x, ai = a[r].y;
+#pragma unroll
+                for (int c = 0; c < KD; ++c) {
+                    const T mv = M[r * KD + c];
+                    ar = fma(mv, nb[c].x, ar);
+                    ai = fma(mv, nb[c].y, ai);
+                }
+                a[r] = mk<T>(ar, ai);
+            }
+        }
+    }
+    C t[KD];
+#pragma unroll
+    for (int c = 0; c < KD; ++c) {
+        t[c].x = __shfl_down_sync(0xffffffffu, a[c].x, 1);
+        t[c].y = __shfl_down_sync(0xffffffffu, a[c].y, 1);
+    }
+    // 3) correction x_B -= G_B t_{B+1}
+    if (B + 1 < P) {
+        for (int i = 0; i < L; ++i) {
+            const int e = B * L + i;
+            if (e >= n) break;
+            const int idx = i * kPitch + B;
+            C x = buf[idx];
+#pragma unroll
+            for (int c = 0; c < KD; ++c) {
+                const T gv = tab.g[(c * L + i) * 32 + B];
+                x.x = fma(-gv, t[c].x, x.x);
+                x.y = fma(-gv, t[c].y, x.y);
+            }
+            buf[idx] = x;
+        }
+    }
+    __syncwarp();
+    for (int p = lane; p < n; p += 32) {
+        const int e = tab.dir ? (n - 1 - p) : p;
+        const int Bq = e / L, i = e - Bq * L;
+        out[base + p] = conv<TO>(buf[i * kPitch + Bq]);
+    }
+}
+
+template <typename T, int KD>
+static cudaError_t solve_kd(const SolveTab<T>& tab, int nrows, const void* in, int in_prec, void* out, int out_prec,
+                            void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
+                            cudaStream_t s) {
+    const size_t smem = (size_t)tab.L * kPitch * sizeof(cx<T>);
+    dim3 grid(nrows), block(32);
+    // in/out/vstore precision combinations used by the runtime
+#define GB_SOLVE_CASE(TI_, TO_, TV_)                                                                             \
+    {                                                                                                            \
+        auto kern = k_solve<T, KD, TI_, TO_, TV_>;                                                               \
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,           \
+                                       check_broken);                                                            \
+        return cudaGetLastError();                                                                               \
+    }
+    const int key = in_prec * 4 + out_prec * 2 + v_prec;
+    switch (key) {
+        case 0: GB_SOLVE_CASE(double2, double2, double2)
+        case 1: GB_SOLVE_CASE(double2, double2, float2)
+        case 2: GB_SOLVE_CASE(double2, float2, double2)
+        case 3: GB_SOLVE_CASE(double2, float2, float2)
+        case 4: GB_SOLVE_CASE(float2, double2, double2)
+        case 5: GB_SOLVE_CASE(float2, double2, float2)
+        case 6: GB_SOLVE_CASE(float2, float2, double2)
+        default: GB_SOLVE_CASE(float2, float2, float2)
+    }
+#undef GB_SOLVE_CASE
+}
+
+template <typename T>
+static cudaError_t solve_dispatch(const SolveTab<T>& tab, int nrows, const void* in, int in_prec, void* out,
+                                  int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode,
+                                  int check_broken, cudaStream_t s) {
+    switch (tab.kd) {
+#define GB_KD(K) \
+    case K: return solve_kd<T, K>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, scale_mode, check_broken, s);
+        GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
+#undef GB_KD
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_solve(int arith, const void* tab, int nrows, const void* in, int in_prec, void* out, int out_prec,
+                         void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
+                         cudaStream_t s) {
+    count_launch();
+    if (arith == 0)
+        return solve_dispatch(*(const SolveTab<double>*)tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl,
+                              scale_mode, check_broken, s);
+    return solve_dispatch(*(const SolveTab<float>*)tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl,
+                          scale_mode, check_broken, s);
+}
+
+// ---------------------------------------------------------------------------
+// tensor-potential matvec over the term list (TensorPotentialMultiply_*_BandNH)
+// ---------------------------------------------------------------------------
+constexpr int kBandTile = 128;
+
+template <typename T>
+__global__ void __launch_bounds__(kBandTile) k_band_apply(BandOp<T> op, const cx<T>* __restrict__ x,
+                                                          cx<T>* __restrict__ y, const SchedEntry* __restrict__ sched,
+                                                          const Ctrl* __restrict__ ctrl, double scal_val,
+                                                          int check_broken) {
+    using C = cx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* sx = reinterpret_cast<C*>(smem_raw);
+    if (check_broken && ctrl->broken) return;
+    const int l = blockIdx.y, i0 = blockIdx.x * kBandTile, tid = threadIdx.x, i = i0 + tid;
+    const int nr = op.nr, kb = op.kb, W = 2 * kb + 1;
+    const double scal = sched ? sched[ctrl->step].scaling : scal_val;
+    T yr = 0, yi = 0;
+    const int t0 = op.row_ptr[l], t1 = op.row_ptr[l + 1];
+    for (int t = t0; t < t1; ++t) {
+        const int src = op.t_src[t];
+        const size_t sbase = (size_t)src * nr;
+        __syncthreads();
+        for (int j = tid; j < kBandTile + 2 * kb; j += kBandTile) {
+            const int g = i0 - kb + j;
+            sx[j] = (g >= 0 && g < nr) ? x[sbase + g] : mk<T>(0, 0);
+        }
+        __syncthreads();
+        if (i < nr) {
+            const T* A = op.slots + (size_t)op.t_slot[t] * W * nr + i;
+            T ar = 0, ai = 0;
+            for (int d = 0; d < W; ++d) {
+                const T a = __ldg(A + (size_t)d * nr);
+                const C v = sx[tid + d];
+                ar = fma(a, v.x, ar);
+                ai = fma(a, v.y, ai);
+            }
+            double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
+            if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
+            const T Cr = (T)cr, Ci = (T)ci;
+            yr += Cr * ar - Ci * ai;
+            yi += Cr * ai + Ci * ar;
+        }
+    }
+    if (i < nr) y[(size_t)l * nr + i] = mk<T>(yr, yi);
+}
+
+cudaError_t launch_band_apply(int arith, const void* opv, const void* x, void* y, const SchedEntry* sched,
+                              const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s) {
+    count_launch();
+    if (arith == 0) {
+        const BandOp<double>& op = *(const BandOp<double>*)opv;
+        dim3 grid((op.nr + kBandTile - 1) / kBandTile, op.nl);
+        size_t smem = (kBandTile + 2 * op.kb) * sizeof(double2);
+        k_band_apply<double><<<grid, kBandTile, smem, s>>>(op, (const double2*)x, (double2*)y, sched, ctrl, scaling,
+                                                           check_broken);
+    } else {
+        const BandOp<float>& op = *(const BandOp<float>*)opv;
+        dim3 grid((op.nr + kBandTile - 1) / kBandTile, op.nl);
+        size_t smem = (kBandTile + 2 * op.kb) * sizeof(float2);
+        k_band_apply<float><<<grid, kBandTile, smem, s>>>(op, (const float2*)x, (float2*)y, sched, ctrl, scaling,
+                                                          check_broken);
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// x <- U x  (ztbmv 'U','N'), elementwise parallel; U diagonal-major ud[d*nr + i] = U(i, i+d)
+// ---------------------------------------------------------------------------
+template <typename T, typename TI, typename TO>
+__global__ void k_tbmv(int kd, const T* __restrict__ ud, int nl, int nr, const TI* __restrict__ in,
+                       TO* __restrict__ out) {
+    const size_t N = (size_t)nl * nr;
+    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < N; g += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(g / nr), i = (int)(g - (size_t)l * nr);
+        const size_t base = (size_t)l * nr;
+        T sr = 0, si = 0;
+        for (int d = 0; d <= kd && i + d < nr; ++d) {
+            const T u = ud[(size_t)d * nr + i];
+            const TI v = in[base + i + d];
+            sr = fma(u, (T)v.x, sr);
+            si = fma(u, (T)v.y, si);
+        }
+        TO o;
+        o.x = (typename elem_of<TO>::type)sr;
+        o.y = (typename elem_of<TO>::type)si;
+        out[g] = o;
+    }
+}
+
+cudaError_t launch_tbmv(int arith, int kd, const void* ud, int nl, int nr, const void* in, int in_prec, void* out,
+                        int out_prec, cudaStream_t s) {
+    count_launch();
+    const size_t N = (size_t)nl * nr;
+    int blocks = (int)((N + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (arith != 0) return cudaErrorInvalidValue;
+    if (in_prec == 0 && out_prec == 0)
+        k_tbmv<double, double2, double2><<<blocks, 256, 0, s>>>(kd, (const double*)ud, nl, nr, (const double2*)in, (double2*)out);
+    else if (in_prec == 1 && out_prec == 0)
+        k_tbmv<double, float2, double2><<<blocks, 256, 0, s>>>(kd, (const double*)ud, nl, nr, (const float2*)in, (double2*)out);
+    else if (in_prec == 1 && out_prec == 1)
+        k_tbmv<double, float2, float2><<<blocks, 256, 0, s>>>(kd, (const double*)ud, nl, nr, (const float2*)in, (float2*)out);
+    else
+        k_tbmv<double, double2, float2><<<blocks, 256, 0, s>>>(kd, (const double*)ud, nl, nr, (const double2*)in, (float2*)out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// reductions: ||x||, Gram-Schmidt projections and updates
+// ---------------------------------------------------------------------------
+constexpr int kRedThreads = 256;
+constexpr int kPStride = 2 * kMaxBasis + 4;   // doubles of partials per block
+constexpr int kKChunk = 8;                    // basis vectors handled per pass over w
+
+int grid_reduce_blocks() { return 152 * 2; }
+
+template <typename CI>
+__global__ void __launch_bounds__(kRedThreads) k_norm(const CI* __restrict__ x, long n, double* partials,
+                                                      unsigned* counter, Ctrl* ctrl) {
+    double acc[1] = {0.0};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const CI v = x[i];
+        const double re = (double)v.x, im = (double)v.y;
+        acc[0] = fma(re, re, acc[0]);
+        acc[0] = fma(im, im, acc[0]);
+    }
+    block_partials<1>(acc, 1, partials, kPStride, 0);
+    if (is_last_block(counter)) {
+        __shared__ double tot[1];
+        final_sum(partials, gridDim.x, kPStride, 1, tot);
+        if (threadIdx.x == 0) {
+            const double b = sqrt(tot[0]);
+            ctrl->beta0 = b;
+            ctrl->beta = b;
+            ctrl->inv_beta = 1.0 / b;
+            if (!isfinite(b) || b == 0.0) ctrl->nonfinite = 1;
+            *counter = 0;
+        }
+    }
+}
+
+cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsigned* counter, Ctrl* ctrl,
+                        cudaStream_t s) {
+    count_launch();
+    const int blocks = grid_reduce_blocks();
+    if (prec == 0) k_norm<double2><<<blocks, kRedThreads, 0, s>>>((const double2*)x, n, partials, counter, ctrl);
+    else k_norm<float2><<<blocks, kRedThreads, 0, s>>>((const float2*)x, n, partials, counter, ctrl);
+    return cudaGetLastError();
+}
+
+// h_k = <v_k, w> for k < nv (BLASIntegrationFunctor block InnerProduct, functors.h:236-240).
+// mode 0 writes ctrl->h (and ||w|| into orig_norm when want_norm), mode 1 writes ctrl->h3
+// and runs only while a re-orthogonalisation pass is requested.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_cgs_dot(const cx<T>* __restrict__ V, long n, int nv,
+                                                         const cx<T>* __restrict__ w, double* partials,
+                                                         unsigned* counter, Ctrl* ctrl, int mode, int want_norm) {
+    using C = cx<T>;
+    if (ctrl->broken) return;
+    if (mode == 1 && !ctrl->ro_go) return;
+    for (int kc = 0; kc < nv; kc += kKChunk) {
+        double acc[2 * kKChunk];
+#pragma unroll
+        for (int k = 0; k < 2 * kKChunk; ++k) acc[k] = 0.0;
+        for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+            const C wi = w[i];
+            // products in the working precision, promoted per element
+#pragma unroll
+            for (int k = 0; k < kKChunk; ++k) {
+                if (kc + k < nv) {
+                    const C v = V[(size_t)(kc + k) * n + i];
+                    const T pr = v.x * wi.x + v.y * wi.y;
+                    const T pi = v.x * wi.y - v.y * wi.x;
+                    acc[2 * k] += (double)pr;
+                    acc[2 * k + 1] += (double)pi;
+                }
+            }
+        }
+        const int nvalid = 2 * min(kKChunk, nv - kc);
+        block_partials<2 * kKChunk>(acc, nvalid, partials, kPStride, 2 * kc);
+    }
+    if (want_norm && mode == 0) {
+        double acc[1] = {0.0};
+        for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+            const C wi = w[i];
+            const double re = (double)wi.x, im = (double)wi.y;
+            acc[0] = fma(re, re, acc[0]);
+            acc[0] = fma(im, im, acc[0]);
+        }
+        block_partials<1>(acc, 1, partials, kPStride, 2 * kMaxBasis);
+    }
+    if (is_last_block(counter)) {
+        __shared__ double tot[2 * kMaxBasis + 1];
+        final_sum(partials, gridDim.x, kPStride, 2 * nv, tot);
+        if (want_norm && mode == 0) {
+            __shared__ double nn[1];
+            final_sum(partials + 2 * kMaxBasis, gridDim.x, kPStride, 1, nn);
+            if (threadIdx.x == 0) ctrl->orig_norm = sqrt(nn[0]);
+        }
+        double* dst = mode ? ctrl->h3 : ctrl->h;
+        for (int k = threadIdx.x; k < 2 * nv; k += blockDim.x) dst[k] = tot[k];
+        if (threadIdx.x == 0) *counter = 0;
+    }
+}
+
+cudaError_t launch_cgs_dot(int prec, const void* V, long n, int nv, const void* w, double* partials, unsigned* counter,
+                           Ctrl* ctrl, int mode, int want_norm, cudaStream_t s) {
+    count_launch();
+    const int blocks = grid_reduce_blocks();
+    if (prec == 0)
+        k_cgs_dot<double><<<blocks, kRedThreads, 0, s>>>((const double2*)V, n, nv, (const double2*)w, partials, counter,
+                                                         ctrl, mode, want_norm);
+    else
+        k_cgs_dot<float><<<blocks, kRedThreads, 0, s>>>((const float2*)V, n, nv, (const float2*)w, partials, counter,
+                                                        ctrl, mode, want_norm);
+    return cudaGetLastError();
+}
+
+// w <- w - V h  (zgemv 'N' + zaxpy, pamp.h:330-332) and ||w||.
+// mode 0: primary pass (h), sets resid_norm and the re-orthogonalisation request
+//         (pamp.h:369: resid < 0.717 * orig) when mode_flags bit 1 (double orth) is set;
+// mode 1: re-orthogonalisation pass (h3), h += h3, orig <- resid, resid <- ||w||.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_cgs_update(const cx<T>* __restrict__ V, long n, int nv,
+                                                            cx<T>* __restrict__ w, double* partials,
+                                                            unsigned* counter, Ctrl* ctrl, int mode) {
+    using C = cx<T>;
+    __shared__ C hs[kMaxBasis];
+    if (ctrl->broken) return;
+    const int pass = mode & 1;
+    const int dorth = (mode >> 1) & 1;
+    if (pass == 1 && !ctrl->ro_go) return;
+    const double* h = pass ? ctrl->h3 : ctrl->h;
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) hs[k] = mk<T>((T)h[2 * k], (T)h[2 * k + 1]);
+    __syncthreads();
+    double acc[1] = {0.0};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        T sr = 0, si = 0;
+        for (int k = 0; k < nv; ++k) {
+            const C v = V[(size_t)k * n + i];
+            const C hk = hs[k];
+            sr = fma(v.x, hk.x, sr);
+            sr = fma(-v.y, hk.y, sr);
+            si = fma(v.x, hk.y, si);
+            si = fma(v.y, hk.x, si);
+        }
+        C r = w[i];
+        r.x -= sr;
+        r.y -= si;
+        w[i] = r;
+        const double re = (double)r.x, im = (double)r.y;
+        acc[0] = fma(re, re, acc[0]);
+        acc[0] = fma(im, im, acc[0]);
+    }
+    block_partials<1>(acc, 1, partials, kPStride, 0);
+    if (is_last_block(counter)) {
+        __shared__ double tot[1];
+        final_sum(partials, gridDim.x, kPStride, 1, tot);
+        if (threadIdx.x == 0) {
+            const double resid = sqrt(tot[0]);
+            if (!isfinite(resid)) ctrl->nonfinite = 1;
+            if (pass == 0) {
+                ctrl->resid_norm = resid;
+                ctrl->ro_count = 0;
+                ctrl->ro_go = dorth && (fabs(resid) < 0.717 * fabs(ctrl->orig_norm));
+            } else {
+                ctrl->orthogonalization_count++;
+                ctrl->ro_count++;
+                ctrl->orig_norm = ctrl->resid_norm;
+                ctrl->resid_norm = resid;
+                // the reference loop runs at most MaxOrthogonalizationCount = 3 passes (pamp.h:75,375)
+                ctrl->ro_go = (fabs(resid) < 0.717 * fabs(ctrl->orig_norm)) ? 1 : 0;
+            }
+            *counter = 0;
+        }
+        if (pass == 1) {
+            __syncthreads();
+            for (int k = threadIdx.x; k < 2 * nv; k += blockDim.x) ctrl->h[k] += ctrl->h3[k];
+        }
+    }
+}
+
+cudaError_t launch_cgs_update(int prec, const void* V, long n, int nv, void* w, double* partials, unsigned* counter,
+                              Ctrl* ctrl, int mode, cudaStream_t s) {
+    count_launch();
+    const int blocks = grid_reduce_blocks();
+    if (prec == 0)
+        k_cgs_update<double><<<blocks, kRedThreads, 0, s>>>((const double2*)V, n, nv, (double2*)w, partials, counter,
+                                                            ctrl, mode);
+    else
+        k_cgs_update<float><<<blocks, kRedThreads, 0, s>>>((const float2*)V, n, nv, (float2*)w, partials, counter,
+                                                           ctrl, mode);
+    return cudaGetLastError();
+}
+
+// Writes Hessenberg column J, the next beta and the happy-breakdown decision
+// (pamp.h:305-315, 345).
+__global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth) {
+    if (ctrl->broken) return;
+    const int nv = J + 1;
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+        H[2 * ((size_t)k * m + J)] = ctrl->h[2 * k];
+        H[2 * ((size_t)k * m + J) + 1] = ctrl->h[2 * k + 1];
+    }
+    if (threadIdx.x == 0) {
+        ctrl->nbasis = nv;
+        ctrl->operator_count++;
+        if (J == 0) ctrl->inner_product_count++;
+        // after the third pass the reference counts once more and stops (pamp.h:372-381)
+        if (double_orth && ctrl->ro_go && ctrl->ro_count >= 3) ctrl->orthogonalization_count++;
+        if (J + 1 < m) {
+            const double beta = ctrl->resid_norm;
+            const double tol = sqrt(DBL_EPSILON);   // pamp.h:79
+            if (!isfinite(beta)) ctrl->nonfinite = 1;
+            if (fabs(beta) < tol) {
+                ctrl->broken = 1;
+                ctrl->breakdown_count++;
+            } else {
+                H[2 * ((size_t)(J + 1) * m + J)] = beta;
+                H[2 * ((size_t)(J + 1) * m + J) + 1] = 0.0;
+                ctrl->beta = beta;
+                ctrl->inv_beta = 1.0 / beta;
+            }
+        }
+    }
+}
+
+cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, cudaStream_t s) {
+    count_launch();
+    k_arnoldi_finalize<<<1, 64, 0, s>>>(ctrl, H, m, J, double_orth);
+    return cudaGetLastError();
+}
+
+__global__ void k_step_begin(Ctrl* ctrl, double* H, int m) {
+    for (int k = threadIdx.x; k < 2 * m * m; k += blockDim.x) H[k] = 0.0;
+    if (threadIdx.x == 0) {
+        ctrl->broken = 0;
+        ctrl->nbasis = 0;
+        ctrl->ro_go = 0;
+        ctrl->ro_count = 0;
+    }
+}
+
+cudaError_t launch_step_begin(Ctrl* ctrl, double* H, int m, cudaStream_t s) {
+    count_launch();
+    k_step_begin<<<1, 256, 0, s>>>(ctrl, H, m);
+    return cudaGetLastError();
+}
+
+__global__ void k_step_end(Ctrl* ctrl) {
+    ctrl->step++;
+    ctrl->step_count++;
+}
+
+cudaError_t launch_step_end(Ctrl* ctrl, cudaStream_t s) {
+    count_launch();
+    k_step_end<<<1, 1, 0, s>>>(ctrl);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Hessenberg exponential: pAMP::ScalingPadeExponential + PadeExponential
+// (pamp.h:430-564), FP64, one CTA.  Matrices are row-major m*m complex in smem.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 cmulz(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ void smem_matmul(int m, const double2* A, const double2* B, double2* Cm) {
+    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+        const int r = idx / m, c = idx - r * m;
+        double sr = 0.0, si = 0.0;
+        for (int k = 0; k < m; ++k) {
+            const double2 a = A[r * m + k], b = B[k * m + c];
+            sr = fma(a.x, b.x, sr);
+            sr = fma(-a.y, b.y, sr);
+            si = fma(a.x, b.y, si);
+            si = fma(a.y, b.x, si);
+        }
+        Cm[idx] = make_double2(sr, si);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ double cabs1d(double2 a) { return fabs(a.x) + fabs(a.y); }
+
+__device__ double2 cdivz(double2 a, double2 b) {
+    // Smith's algorithm
+    if (fabs(b.x) >= fabs(b.y)) {
+        const double q = b.y / b.x, d = b.x + b.y * q;
+        return make_double2((a.x + a.y * q) / d, (a.y - a.x * q) / d);
+    }
+    const double q = b.x / b.y, d = b.y + b.x * q;
+    return make_double2((a.x * q + a.y) / d, (a.y * q - a.x) / d);
+}
+
+__global__ void __launch_bounds__(256) k_expm(Ctrl* ctrl, double* Hg, int m, const SchedEntry* sched) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int mm = m * m;
+    double2* A = reinterpret_cast<double2*>(smem_raw);
+    double2* A2 = A + mm;
+    double2* P = A2 + mm;
+    double2* Q = P + mm;
+    double2* T = Q + mm;
+    __shared__ double red[8];
+    __shared__ int piv[kMaxBasis];
+    __shared__ int s_p;
+    __shared__ double s_c[8];
+    const int tid = threadIdx.x;
+    const SchedEntry se = sched[ctrl->step];
+    // HessenbergMatrix *= -dt * i   (pamp.h:634), kept in global for GetHessenbergMatrix
+    const double2 f = make_double2(se.dt_im, -se.dt_re);
+    double mx = 0.0;
+    for (int k = tid; k < mm; k += blockDim.x) {
+        const double2 h = make_double2(Hg[2 * k], Hg[2 * k + 1]);
+        const double2 a = cmulz(h, f);
+        Hg[2 * k] = a.x;
+        Hg[2 * k + 1] = a.y;
+        A[k] = a;
+        mx = fmax(mx, hypot(a.x, a.y));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) red[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, red[w]);
+        int s = v > 0.0 ? (int)ceil(log2(v)) : 0;
+        if (s < 0) s = 0;
+        s_p = s;
+        // Pade coefficients, order 6 (pamp.h:491-495)
+        const int order = 6;
+        s_c[0] = 1.0;
+        for (int i = 0; i < order; ++i) s_c[i + 1] = s_c[i] * (double)(order - i) / (double)((i + 1) * (2 * order - i));
+    }
+    __syncthreads();
+    const int sorder = s_p;
+    const double sc = pow(2.0, (double)sorder);
+    for (int k = tid; k < mm; k += blockDim.x) { A[k].x /= sc; A[k].y /= sc; }
+    __syncthreads();
+    smem_matmul(m, A, A, A2);
+    // Horner in A^2 (pamp.h:497-539).  The first product of each polynomial is
+    // with a scalar multiple of I and is formed directly (exactly equal).
+    const int order = 6;
+    for (int k = tid; k < mm; k += blockDim.x) {
+        Q[k] = make_double2(s_c[order] * A2[k].x, s_c[order] * A2[k].y);       // i = 4 (odd step)
+        P[k] = make_double2(s_c[order - 1] * A2[k].x, s_c[order - 1] * A2[k].y); // i = 3
+    }
+    __syncthreads();
+    for (int r = tid; r < m; r += blockDim.x) { Q[r * m + r].x += s_c[4]; P[r * m + r].x += s_c[3]; }
+    __syncthreads();
+    // i = 2: Q = Q A2 + c2 I ; i = 1: P = P A2 + c1 I ; i = 0: Q = Q A2 + c0 I
+    smem_matmul(m, Q, A2, T);
+    for (int k = tid; k < mm; k += blockDim.x) Q[k] = T[k];
+    __syncthreads();
+    for (int r = tid; r < m; r += blockDim.x) Q[r * m + r].x += s_c[2];
+    __syncthreads();
+    smem_matmul(m, P, A2, T);
+    for (int k = tid; k < mm; k += blockDim.x) P[k] = T[k];
+    __syncthreads();
+    for (int r = tid; r < m; r += blockDim.x) P[r * m + r].x += s_c[1];
+    __syncthreads();
+    smem_matmul(m, Q, A2, T);
+    for (int k = tid; k < mm; k += blockDim.x) Q[k] = T[k];
+    __syncthreads();
+    for (int r = tid; r < m; r += blockDim.x) Q[r * m + r].x += s_c[0];
+    __syncthreads();
+    // odd == false at loop end for order 6: P = P A (pamp.h:530-539)
+    smem_matmul(m, P, A, T);
+    for (int k = tid; k < mm; k += blockDim.x) {
+        P[k] = T[k];
+        Q[k] = make_double2(Q[k].x - T[k].x, Q[k].y - T[k].y);   // Q = Q - P
+    }
+    __syncthreads();
+    // zgetrf: LU with partial pivoting on |re|+|im| (first maximum), rows swapped whole
+    int info = 0;
+    for (int k = 0; k < m; ++k) {
+        if (tid < 32) {
+            double best = -1.0;
+            int bi = k;
+            for (int r = k + tid; r < m; r += 32) {
+                const double v = cabs1d(Q[r * m + k]);
+                if (v > best) { best = v; bi = r; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (tid == 0) { piv[k] = bi; s_p = (best == 0.0) ? -1 : bi; }
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p < 0) { if (!info) info = k + 1; __syncthreads(); continue; }
+        if (p != k)
+            for (int c = tid; c < m; c += blockDim.x) {
+                const double2 t = Q[k * m + c];
+                Q[k * m + c] = Q[p * m + c];
+                Q[p * m + c] = t;
+            }
+        __syncthreads();
+        const double2 inv = cdivz(make_double2(1.0, 0.0), Q[k * m + k]);
+        for (int r = k + 1 + tid; r < m; r += blockDim.x) Q[r * m + k] = cmulz(Q[r * m + k], inv);
+        __syncthreads();
+        const int rem = m - k - 1;
+        for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
+            const int r = k + 1 + idx / rem, c = k + 1 + idx % rem;
+            const double2 fr = Q[r * m + k], u = Q[k * m + c];
+            double2 q = Q[r * m + c];
+            q.x -= fr.x * u.x - fr.y * u.y;
+            q.y -= fr.x * u.y + fr.y * u.x;
+            Q[r * m + c] = q;
+        }
+        __syncthreads();
+    }
+    if (info) {
+        if (tid == 0) ctrl->lu_info = info;
+    } else {
+        // zgetrs 'N': apply the row interchanges to P, then L y = b, U x = y (column-parallel axpy form)
+        for (int k = 0; k < m; ++k) {
+            const int p = piv[k];
+            if (p != k)
+                for (int c = tid; c < m; c += blockDim.x) {
+                    const double2 t = P[k * m + c];
+                    P[k * m + c] = P[p * m + c];
+                    P[p * m + c] = t;
+                }
+            __syncthreads();
+        }
+        for (int r = 0; r < m; ++r) {
+            for (int idx = tid; idx < (m - r - 1) * m; idx += blockDim.x) {
+                const int rr = r + 1 + idx / m, c = idx % m;
+                const double2 lf = Q[rr * m + r], x = P[r * m + c];
+                double2 b = P[rr * m + c];
+                b.x -= lf.x * x.x - lf.y * x.y;
+                b.y -= lf.x * x.y + lf.y * x.x;
+                P[rr * m + c] = b;
+            }
+            __syncthreads();
+        }
+        for (int r = m - 1; r >= 0; --r) {
+            for (int c = tid; c < m; c += blockDim.x) P[r * m + c] = cdivz(P[r * m + c], Q[r * m + r]);
+            __syncthreads();
+            for (int idx = tid; idx < r * m; idx += blockDim.x) {
+                const int rr = idx / m, c = idx % m;
+                const double2 uf = Q[rr * m + r], x = P[r * m + c];
+                double2 b = P[rr * m + c];
+                b.x -= uf.x * x.x - uf.y * x.y;
+                b.y -= uf.x * x.y + uf.y * x.x;
+                P[rr * m + c] = b;
+            }
+            __syncthreads();
+        }
+    }
+    // output = I + 2 P  (not negated: odd == false for order 6)
+    for (int k = tid; k < mm; k += blockDim.x) A[k] = make_double2(2.0 * P[k].x, 2.0 * P[k].y);
+    __syncthreads();
+    for (int r = tid; r < m; r += blockDim.x) A[r * m + r].x += 1.0;
+    __syncthreads();
+    for (int i = 0; i < sorder; ++i) {
+        smem_matmul(m, A, A, T);
+        for (int k = tid; k < mm; k += blockDim.x) A[k] = T[k];
+        __syncthreads();
+    }
+    for (int k = tid; k < m; k += blockDim.x) {
+        ctrl->y[2 * k] = A[k * m].x;
+        ctrl->y[2 * k + 1] = A[k * m].y;
+    }
+    if (tid == 0) {
+        const double2 yl = A[(m - 1) * m];
+        ctrl->err_est = yl.x * yl.x + yl.y * yl.y;
+        ctrl->scaling_order = sorder;
+    }
+}
+
+cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s) {
+    count_launch();
+    const size_t smem = (size_t)5 * m * m * sizeof(double2);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_expm<<<1, 256, smem, s>>>(ctrl, H, m, sched);
+    return cudaGetLastError();
+}
+
+// psi = beta0 * V y  (pamp.h:657-662), FP64 accumulation, complex128 output.
+template <typename T>
+__global__ void k_combine(const cx<T>* __restrict__ V, long n, const Ctrl* __restrict__ ctrl, double2* __restrict__ out) {
+    __shared__ double2 ys[kMaxBasis];
+    const int nb = ctrl->nbasis;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) ys[k] = make_double2(ctrl->y[2 * k], ctrl->y[2 * k + 1]);
+    __syncthreads();
+    const double b0 = ctrl->beta0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double sr = 0.0, si = 0.0;
+        for (int k = 0; k < nb; ++k) {
+            const cx<T> v = V[(size_t)k * n + i];
+            const double vr = (double)v.x, vi = (double)v.y;
+            sr = fma(vr, ys[k].x, sr);
+            sr = fma(-vi, ys[k].y, sr);
+            si = fma(vr, ys[k].y, si);
+            si = fma(vi, ys[k].x, si);
+        }
+        out[i] = make_double2(sr * b0, si * b0);
+    }
+}
+
+cudaError_t launch_combine(int prec, const void* V, long n, const Ctrl* ctrl, void* out, cudaStream_t s) {
+    count_launch();
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (prec == 0) k_combine<double><<<blocks, 256, 0, s>>>((const double2*)V, n, ctrl, (double2*)out);
+    else k_combine<float><<<blocks, 256, 0, s>>>((const float2*)V, n, ctrl, (double2*)out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// stateless reference-storage kernel: TensorPotentialMultiply_{Diag,Simp}_BandNH
+// V complex band in BLAS storage (element (i,j) at j*(2kb+1) + kb + i - j)
+// ---------------------------------------------------------------------------
+__global__ void k_tensor_multiply_ref(int storage, const double2* __restrict__ V, int npairs,
+                                      const int* __restrict__ pairs, int kb, double scaling,
+                                      const double2* __restrict__ src, double2* __restrict__ dst, int nl, int nr) {
+    const int l = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nr) return;
+    const int W = 2 * kb + 1;
+    double sr = 0.0, si = 0.0;
+    const int j0 = max(0, i - kb), j1 = min(nr - 1, i + kb);
+    auto band = [&](const double2* A, const double2* x) {
+        for (int j = j0; j <= j1; ++j) {
+            const double2 a = A[(size_t)j * W + kb + i - j];
+            const double2 v = x[j];
+            sr += a.x * v.x - a.y * v.y;
+            si += a.x * v.y + a.y * v.x;
+        }
+    };
+    if (storage == 0) {
+        band(V + (size_t)l * W * nr, src + (size_t)l * nr);
+    } else {
+        for (int p = 0; p < npairs; ++p) {
+            if (pairs[2 * p] != l) continue;
+            band(V + (size_t)p * W * nr, src + (size_t)pairs[2 * p + 1] * nr);
+        }
+    }
+    double2 d = dst[(size_t)l * nr + i];
+    d.x += scaling * sr;
+    d.y += scaling * si;
+    dst[(size_t)l * nr + i] = d;
+}
+
+cudaError_t launch_tensor_multiply_ref(int storage, const double2* V, int npairs, const int* pairs, int kb,
+                                       double scaling, const double2* src, double2* dst, int nl, int nr,
+                                       cudaStream_t s) {
+    count_launch();
+    dim3 grid((nr + 127) / 128, nl);
+    k_tensor_multiply_ref<<<grid, 128, 0, s>>>(storage, V, npairs, pairs, kb, scaling, src, dst, nl, nr);
+    return cudaGetLastError();
+}
+
+__global__ void k_zero(unsigned char* p, size_t bytes) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < bytes; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = 0;
+}
+
+cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s) {
+    count_launch();
+    k_zero<<<64, 256, 0, s>>>((unsigned char*)p, bytes);
+    return cudaGetLastError();
+}
+
+}  // namespace gbprop
