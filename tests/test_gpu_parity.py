@@ -1,0 +1,244 @@
+"""GPU parity: libgbprop (through the C ABI) against the CPU oracle on the
+same seeded inputs.  FP64 tolerances are written per test; the headline bar is
+<= 1e-11 relative L2 on the final wavefunction of the 500-step workload."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import make_problem, rel, scalings_for
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "oracle_small.npz")
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _dev(a, dtype=None):
+    torch = _torch()
+    return torch.as_tensor(np.ascontiguousarray(a)).to("cuda", dtype=dtype)
+
+
+def _host(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def small():
+    import pyprop_gb300 as pp
+    conf = pp.Load(os.path.join(os.path.dirname(__file__), "..", "pyprop_gb300", "configs",
+                                "hydrogen_velocity_small.ini"))
+    prob = pp.Problem(conf)
+    prob.SetupStep()
+    return prob
+
+
+def test_balanced_matvec_vs_oracle(small):
+    op = orc.Operator.from_problem(small)
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal((op.nl, op.nr)) + 1j * rng.standard_normal((op.nl, op.nr))
+    for s in (0.0, 0.731):
+        want = op.balanced_matvec(x, s)
+        src = _dev(x)
+        dst = _torch().zeros_like(src)
+        small.Propagator.Handle().matvec(src, dst, s, balanced=True)
+        assert rel(_host(dst), want) < 1e-13
+        assert np.array_equal(_host(src), x)          # source untouched
+        want2 = op.multiply_potentials(x, s)
+        small.Propagator.Handle().matvec(src, dst, s, balanced=False)
+        assert rel(_host(dst), want2) < 1e-14
+
+
+def test_sqrt_overlap_ops_vs_oracle(small):
+    op = orc.Operator.from_problem(small)
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal((op.nl, op.nr)) + 1j * rng.standard_normal((op.nl, op.nr))
+    h = small.Propagator.Handle()
+    d = _dev(x)
+    h.multiply_sqrt_overlap(d)
+    assert rel(_host(d), op.multiply_sqrt_overlap(x)) < 1e-15
+    for conj in (False, True):
+        d = _dev(x)
+        h.solve_sqrt_overlap(conj, d)
+        assert rel(_host(d), op.solve_sqrt_overlap(x, conj=conj)) < 1e-13
+
+
+def test_stateless_tensor_multiply_vs_oracle(small):
+    from pyprop_gb300 import _native
+    L = _native.lib()
+    op = orc.Operator.from_problem(small)
+    rng = np.random.default_rng(13)
+    x = rng.standard_normal((op.nl, op.nr)) + 1j * rng.standard_normal((op.nl, op.nr))
+    y0 = rng.standard_normal((op.nl, op.nr)) + 1j * rng.standard_normal((op.nl, op.nr))
+    for kind, td, npairs, pairs, data in op.pots:
+        s = 0.4 if td else 1.0
+        single = orc.Operator(op.nl, op.nr, op.kd, op.kb, op.U,
+                              [dict(kind=kind, data=data, pairs=pairs if kind else None, timedep=False)])
+        want = y0 + single.multiply_potentials(x, 1.0) * s
+        V, src, dst, pr = _dev(data), _dev(x), _dev(y0), _dev(pairs)
+        storage = _native.STORAGE_DIAG if kind == orc.ORC_DIAG_BANDNH else _native.STORAGE_SIMP
+        _native.check(L.gbprop_tensor_multiply_bandnh(storage, _native.ptr(V), npairs, _native.ptr(pr), op.kb, s,
+                                                      _native.ptr(src), _native.ptr(dst), op.nl, op.nr, None))
+        _torch().cuda.synchronize()
+        assert rel(_host(dst), want) < 1e-14
+
+
+def test_single_step_and_hessenberg_vs_oracle(small):
+    op = orc.Operator.from_problem(small)
+    prob = small
+    psi0 = prob.psi.GetDataNumpy().copy()
+    s = 0.3
+    m = prob.Propagator.BasisSize
+    x0 = op.multiply_sqrt_overlap(psi0)
+    xo, Ho, sto = op.pamp_once(x0, m, prob.TimeStep, s)
+    want = op.solve_sqrt_overlap(xo)
+    h = prob.Propagator.Handle()
+    h.reset_stats()
+    d = _dev(psi0)
+    h.advance(d, [s], prob.TimeStep)
+    got = _host(d)
+    assert rel(got, want) < 1e-12
+    Hg = h.hessenberg()
+    assert rel(Hg, Ho) < 1e-12
+    st = h.stats()
+    assert st.operator_count == m and st.step_count == 1 and st.last_basis_size == m
+    assert st.last_scaling_order == sto.last_scaling
+    assert abs(st.error_estimate - sto.error_estimate) <= 1e-6 * max(sto.error_estimate, 1e-300) + 1e-30
+
+
+def test_500_step_workload_vs_oracle():
+    """The CPU-runnable workload end to end through Problem.Advance: <= 1e-11 relative L2."""
+    import pyprop_gb300 as pp
+    g = np.load(GOLD)
+    conf = pp.Load(os.path.join(os.path.dirname(__file__), "..", "pyprop_gb300", "configs",
+                                "hydrogen_velocity_small.ini"))
+    prob = pp.Problem(conf)
+    prob.SetupStep()
+    assert rel(prob.psi.GetDataNumpy(), g["psi0"]) == 0.0
+    assert np.allclose(scalings_for(prob, 500), g["scalings"], rtol=0, atol=0)
+    for _ in prob.Advance(5):
+        pass
+    assert abs(prob.PropagatedTime - 5.0) < 1e-9
+    err = rel(prob.psi.GetDataNumpy(), g["psi500"])
+    print("500-step FP64 relative L2 vs oracle: %.3e" % err)
+    assert err <= 1e-11
+    # live oracle on the same inputs agrees with the committed fixture
+    op = orc.Operator.from_problem(prob)
+    live, _ = op.advance(g["psi0"], int(g["m"]), complex(g["dt"]), g["scalings"][:20])
+    assert rel(live, g["psi20"]) < 1e-12
+
+
+def test_determinism_bitwise(small):
+    h = small.Propagator.Handle()
+    psi0 = small.psi.GetDataNumpy().copy()
+    outs = []
+    for _ in range(2):
+        d = _dev(psi0)
+        h.advance(d, [0.2, 0.25, 0.3], small.TimeStep)
+        outs.append(_host(d))
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 7])
+def test_small_krylov_sizes(m):
+    prob = make_problem(maxl=2, xsize=14, m=m)
+    op = orc.Operator.from_problem(prob)
+    psi0 = prob.psi.GetDataNumpy().copy()
+    scal = [0.0, 0.5, -0.3]
+    want, _ = op.advance(psi0, m, prob.TimeStep, scal)
+    d = _dev(psi0)
+    prob.Propagator.Handle().advance(d, scal, prob.TimeStep)
+    assert rel(_host(d), want) < 1e-12
+
+
+@pytest.mark.parametrize("maxl,xsize,order", [(0, 12, 7), (1, 9, 3), (5, 41, 5), (4, 100, 9), (3, 250, 7)])
+def test_ragged_sizes(maxl, xsize, order):
+    """nl = 1 (no dipole pairs), tiny radial sizes (blocks shorter than the band),
+    odd sizes and orders 3..9."""
+    prob = make_problem(maxl=maxl, xsize=xsize, order=order, m=6)
+    op = orc.Operator.from_problem(prob)
+    psi0 = prob.psi.GetDataNumpy().copy()
+    scal = [0.1, 0.2]
+    want, _ = op.advance(psi0, 6, prob.TimeStep, scal)
+    d = _dev(psi0)
+    prob.Propagator.Handle().advance(d, scal, prob.TimeStep)
+    assert rel(_host(d), want) < 1e-12
+
+
+def test_double_orthogonalization_vs_oracle():
+    prob = make_problem(maxl=3, xsize=30, m=12, dorth=True)
+    op = orc.Operator.from_problem(prob)
+    psi0 = prob.psi.GetDataNumpy().copy()
+    scal = [0.3, 0.3]
+    want, sto = op.advance(psi0, 12, prob.TimeStep, scal, double_orth=True)
+    h = prob.Propagator.Handle()
+    h.reset_stats()
+    d = _dev(psi0)
+    h.advance(d, scal, prob.TimeStep)
+    assert rel(_host(d), want) < 1e-12
+    assert h.stats().orthogonalization_count == sto.orthogonalization_count
+
+
+def test_imaginary_time_step_vs_oracle():
+    prob = make_problem(maxl=2, xsize=30, m=10, dt="-0.01j", potentials=["RadialKineticEnergy", "CoulombPotential"])
+    op = orc.Operator.from_problem(prob)
+    psi0 = prob.psi.GetDataNumpy().copy()
+    want, _ = op.advance(psi0, 10, -0.01j, [1.0] * 3)
+    d = _dev(psi0)
+    prob.Propagator.Handle().advance(d, [1.0] * 3, -0.01j)
+    assert rel(_host(d), want) < 1e-12
+
+
+def test_happy_breakdown_on_gpu():
+    """Two-level start vector of a diagonal operator: the Krylov space closes after 2 vectors."""
+    from pyprop_gb300 import _native
+    nl, nr, kd, kb = 1, 8, 1, 1
+    W = 2 * kb + 1
+    U = np.zeros(nr * (kd + 1))
+    for j in range(nr):
+        U[j * (kd + 1) + kd] = 1.0
+    data = np.zeros((1, W * nr), dtype=np.complex128)
+    diag = np.arange(nr, dtype=float)
+    for i in range(nr):
+        data[0, i * W + kb] = diag[i]
+    h = _native.Handle(nl, nr, _native.FP64, 6, 0, False, 0)
+    h.set_overlap(kd, U)
+    h.add_potential(_native.STORAGE_DIAG, None, kb, data, False)
+    h.finalize()
+    psi = np.zeros((1, nr), dtype=np.complex128)
+    psi[0, 2] = psi[0, 5] = 1.0
+    d = _dev(psi)
+    h.advance(d, [0.0], 0.1)
+    st = h.stats()
+    assert st.breakdown_count == 1 and st.last_basis_size == 2
+    assert np.allclose(_host(d), psi * np.exp(-1j * 0.1 * diag), atol=1e-12)
+
+
+def test_host_buffer_entry_point(small):
+    g = np.load(GOLD)
+    h = small.Propagator.Handle()
+    psi = np.ascontiguousarray(g["psi0"]).copy()
+    h.advance_host(psi, g["scalings"][:20], complex(g["dt"]))
+    assert rel(psi, g["psi20"]) < 1e-12
+
+
+def test_mixed_precision_error_report():
+    """FP32-mixed (complex64 basis/matvec/state, FP64 reductions/expm): error vs the FP64 oracle."""
+    import pyprop_gb300 as pp
+    g = np.load(GOLD)
+    conf = pp.Load(os.path.join(os.path.dirname(__file__), "..", "pyprop_gb300", "configs",
+                                "hydrogen_velocity_small.ini"))
+    conf.Propagation.Set("krylov_precision", "fp32-mixed")
+    prob = pp.Problem(conf)
+    prob.SetupStep()
+    assert prob.psi.GetData().dtype == _torch().complex64
+    for _ in prob.Advance(1):
+        pass
+    err = rel(prob.psi.GetDataNumpy().astype(np.complex128), g["psi500"])
+    print("500-step FP32-mixed relative L2 vs FP64 oracle: %.3e" % err)
+    assert err < 1e-4
