@@ -1,0 +1,366 @@
+"""Benchmark: Krylov steps/s of pyprop's PamPropagator step on GB300.
+
+Workload (default): hydrogen in a velocity-gauge sin^2 pulse at scale,
+l = 0..63 x 1000 B-splines (order 7, exponential-linear breakpoints to 400 a.u.),
+complex128, pAMP m = 30, dt = 0.005 -- pyprop_gb300/configs/hydrogen_velocity_large.ini.
+Inputs are synthetic (seeded complex Gaussian coefficients, random-free operator).
+
+One bench "step" = one PamPropagator.AdvanceStep (psi <- U^-1 pAMP(U psi)).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32-mixed]
+    python bench.py --impl reference ...     # CPU restatement of the reference, host cores
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "large": os.path.join(ROOT, "pyprop_gb300", "configs", "hydrogen_velocity_large.ini"),
+    "small": os.path.join(ROOT, "pyprop_gb300", "configs", "hydrogen_velocity_small.ini"),
+}
+METRIC = "Krylov steps/s (pAMP x TensorPotential step, 1 GB300)"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+# FP64 FMA issue rate measured on this machine's GB300 (profiles/fp64_fp32_issue_rates.md)
+FP64_PEAK_TFLOPS = 1.195
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._proc = None
+        self._thr = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                           "--format=csv,noheader,nounits", "-lms", "200"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._proc = None
+            return
+
+        def reader():
+            for line in self._proc.stdout:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 8:
+                    self.samples.append(parts)
+
+        self._thr = threading.Thread(target=reader, daemon=True)
+        self._thr.start()
+
+    def stop(self):
+        if self._proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self._proc.terminate()
+        try:
+            self._proc.wait(timeout=2)
+        except Exception:
+            self._proc.kill()
+        if self._thr:
+            self._thr.join(timeout=1)
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[4 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def load_peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def algorithmic_bytes(N, m, s, coef_bytes):
+    """Per matvec: 2*N*s + B_coef; per Krylov step: s*N*(m^2 + 7m + 3) + m*B_coef."""
+    return 2 * N * s + coef_bytes, s * N * (m * m + 7 * m + 3) + m * coef_bytes
+
+
+def operator_slots(prob):
+    """(band slots, terms) of the device operator: one real band per stored angular
+    slot and non-zero part (real / imaginary) of each consolidated TensorPotential."""
+    nslots = 0
+    nterms = 0
+    nl = prob.psi.GetRepresentation().angular.count
+    for p in prob.Propagator.BasePropagator.PotentialList:
+        parts = int(np.any(p.PotentialData.real != 0)) + int(np.any(p.PotentialData.imag != 0))
+        nslots += parts * p.PotentialData.shape[0]
+        nterms += parts * (nl if p.GetStorageIds()[0] == "Ident" else p.PotentialData.shape[0])
+    return nslots, nterms
+
+
+def coef_bytes_of(prob, real_elem):
+    """Operator bytes one balanced matvec must read: the real band slots and the
+    parallel-solve tables of U^-1 and U^-T (diagonals, reciprocal diagonal,
+    coupling columns; the small scan operators are left out)."""
+    rad = prob.psi.GetRepresentation().radial
+    nr, kd = rad.count, rad.kd
+    nslots, _ = operator_slots(prob)
+    W = 2 * kd + 1
+    band = nslots * W * nr * real_elem
+    solve = 2 * (kd + 1 + kd) * nr * real_elem
+    return band, solve
+
+
+def build_problem(workload, precision, device):
+    import pyprop_gb300 as pp
+    conf = pp.Load(CONFIGS[workload])
+    conf.Propagation.Set("krylov_precision", precision)
+    prob = pp.Problem(conf, device=device)
+    prob.SetupStep()
+    return prob
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the reference step (oracle/), all host threads."""
+    if rank != 0:
+        return
+    import pyprop_gb300 as pp
+    from oracle import oracle as orc
+    conf = pp.Load(CONFIGS[args.workload])
+    prob = pp.Problem(conf, device="cpu")
+    prob.SetupWavefunction()
+    op = orc.Operator.from_problem(prob)
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    psi = prob.psi.GetDataNumpy().astype(np.complex128)
+    m = prob.Propagator.BasisSize
+    dt = prob.TimeStep
+    bp = prob.Propagator.BasePropagator
+    t = prob.PropagatedTime
+    for _ in range(args.warmup):
+        psi, _ = op.advance(psi, m, dt, [bp._scaling(t)])
+        t = prob._next_time(t)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        psi, _ = op.advance(psi, m, dt, [bp._scaling(t)])
+        t = prob._next_time(t)
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    nl, nr = prob.psi.GetRepresentation().GetFullShape()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": "hydrogen_velocity_%s" % args.workload, "nl": nl, "nr": nr, "order": 7, "m": m,
+                   "dt": dt.real, "precision": "fp64"},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d full Krylov steps of the workload (oracle/oracle.c, OpenMP)" % args.steps},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(workload, budget_s=12.0):
+    """Oracle steps/s on the host cores, on a bounded sample of the same workload."""
+    import pyprop_gb300 as pp
+    from oracle import oracle as orc
+    conf = pp.Load(CONFIGS[workload])
+    prob = pp.Problem(conf, device="cpu")
+    prob.SetupWavefunction()
+    op = orc.Operator.from_problem(prob)
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    psi = prob.psi.GetDataNumpy().astype(np.complex128)
+    m, dt = prob.Propagator.BasisSize, prob.TimeStep
+    psi, _ = op.advance(psi, m, dt, [0.0])          # warm
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and n < 2000:
+        psi, _ = op.advance(psi, m, dt, [0.0])
+        n += 1
+    el = time.perf_counter() - t0
+    return {"value": n / el, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": "%d Krylov steps of the workload in %.1f s (oracle/oracle.c, OpenMP)" % (n, el)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbprop", choices=["gbprop", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32-mixed"])
+    ap.add_argument("--workload", default="large", choices=list(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--flush-mb", type=int, default=512)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "gbprop" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    from pyprop_gb300 import _native
+    device = "cuda:%d" % local
+    torch.cuda.set_device(local)
+
+    prob = build_problem(args.workload, args.precision, device)
+    h = prob.Propagator.Handle()
+    nl, nr = prob.psi.GetRepresentation().GetFullShape()
+    N = nl * nr
+    m = prob.Propagator.BasisSize
+    elem = 16 if args.precision == "fp64" else 8
+    dt = prob.TimeStep
+    bp = prob.Propagator.BasePropagator
+    psi0 = prob.psi.GetData().clone()
+
+    # --- device-resident timing: K steps, L2 flushed between steps ---------------------------
+    flush = torch.empty(args.flush_mb * (1 << 20) // 4, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        prob.AdvanceStep()
+    torch.cuda.synchronize()
+    _barrier(world)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = _native.launch_count()
+    torch.cuda.synchronize()
+    _barrier(world)
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        starts[k].record(stream)
+        prob.AdvanceStep()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    _barrier(world)
+    launches = _native.launch_count() - launches0
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    clk = clocks.stop()
+    ms = _max_over_ranks(ms, world)
+    value = world * args.steps / (ms / 1e3)
+
+    # --- e2e through the C ABI with host buffers (H2D psi, step, D2H psi per step) -----------
+    psi_host = np.ascontiguousarray(prob.psi.GetDataNumpy())
+    scal = np.array([bp._scaling(prob.PropagatedTime)])
+    for _ in range(2):
+        h.advance_host(psi_host, scal, dt)
+    _barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        h.advance_host(psi_host, scal, dt)
+    e2e_s = _max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": world * args.steps / e2e_s, "unit": "steps/s",
+           "h2d_bytes_per_step": psi_host.nbytes, "d2h_bytes_per_step": psi_host.nbytes}
+
+    # --- matvec alone: the tensor-potential kernel and the balanced matvec -------------------
+    band_coef, solve_coef = coef_bytes_of(prob, 8 if args.precision == "fp64" else 4)
+    B_mv, B_step = algorithmic_bytes(N, m, elem, band_coef + solve_coef)
+    src = psi0.clone()
+    dst = torch.empty_like(src)
+    reps = 50
+    for balanced in (0, 1):
+        for _ in range(5):
+            h.matvec(src, dst, 0.1, balanced=bool(balanced))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            h.matvec(src, dst, 0.1, balanced=bool(balanced))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if balanced:
+            t_bal = e0.elapsed_time(e1) / reps
+        else:
+            t_band = e0.elapsed_time(e1) / reps
+    peak, peak_kind = load_peaks()
+    band_bytes = 2 * N * elem + band_coef
+    achieved = band_bytes / (t_band * 1e-3) / 1e9
+    # arithmetic of the band kernel: 2 FMA (4 flops) per real band entry per complex element
+    _, nterms = operator_slots(prob)
+    band_flops = nterms * nr * (2 * prob.psi.GetRepresentation().radial.kd + 1) * 4
+    compute = {"unit": "TFLOP/s", "achieved": band_flops / (t_band * 1e-3) / 1e12,
+               "peak": FP64_PEAK_TFLOPS if args.precision == "fp64" else 69.9,
+               "peak_source": "measured FMA issue rate (profiles/fp64_fp32_issue_rates.md)"}
+    compute["frac"] = compute["achieved"] / compute["peak"]
+    roofline = {
+        "bound": "hbm", "kernel": "k_band_apply (TensorPotentialMultiply, all terms)",
+        "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+        "traffic": None, "launch_ms": t_band,
+        "algorithmic_bytes_per_launch": band_bytes,
+        "compute": compute,
+    }
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+f64",
+        "data": "synthetic",
+        "config": {"workload": "hydrogen_velocity_%s" % args.workload, "nl": nl, "nr": nr, "order": 7, "m": m,
+                   "dt": dt.real, "precision": args.precision, "l2": "flushed between steps (%d MB write)" % args.flush_mb,
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": e2e,
+        "roofline": roofline,
+        "step_bytes": {"algorithmic_per_step": B_step, "achieved_GBps": B_step * value / world / 1e9,
+                       "per_matvec": B_mv},
+        "matvec_ms": {"band_apply": t_band, "balanced": t_bal},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(args.workload)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
