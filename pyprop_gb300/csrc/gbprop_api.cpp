@@ -339,9 +339,23 @@ gbprop_status check_handle(gbprop_handle h, bool need_final) {
         if (_e != cudaSuccess) return fail(GBPROP_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
     } while (0)
 
-const void* ktab(gbprop_ctx* h, int which) {
-    return h->prec == GBPROP_FP64 ? (const void*)&h->t64.tab[which] : (const void*)&h->t32.tab[which];
+// Triangular solve of the Krylov precision: FP64-accurate (FP32 solve + FP64 refinement)
+// for the FP64 path, plain complex64 for the mixed path's basis.
+cudaError_t ksolve(gbprop_ctx* h, int dir, const void* in, int in_prec, void* out, int out_prec, void* vstore,
+                   int v_prec, int scale_mode, int check_broken) {
+    if (h->prec == GBPROP_FP64)
+        return launch_solve_ir(&h->t32.tab[dir], h->d_ud_phys, h->nl, in, in_prec, out, out_prec, vstore, v_prec,
+                               h->d_ctrl, scale_mode, check_broken, h->stream);
+    return launch_solve(1, &h->t32.tab[dir], h->nl, in, in_prec, out, out_prec, vstore, v_prec, h->d_ctrl,
+                        scale_mode, check_broken, h->stream);
 }
+
+// FP64-accurate solve of the state transforms (both precisions).
+cudaError_t ssolve(gbprop_ctx* h, int dir, const void* in, int in_prec, void* out, int out_prec) {
+    return launch_solve_ir(&h->t32.tab[dir], h->d_ud_phys, h->nl, in, in_prec, out, out_prec, nullptr, 0, h->d_ctrl, 0,
+                           0, h->stream);
+}
+
 const void* kop(gbprop_ctx* h) {
     return h->prec == GBPROP_FP64 ? (const void*)&h->t64.op : (const void*)&h->t32.op;
 }
@@ -362,11 +376,11 @@ gbprop_status enqueue_step(gbprop_ctx* h, void* psi) {
         const void* in = J == 0 ? (const void*)h->d_x : (const void*)h->d_r;
         const int in_prec = J == 0 ? 0 : kp;
         // v_J = r / beta_J stored in V[J]; s = U^-1 v_J
-        GB_LAUNCH(launch_solve(kp, ktab(h, 0), h->nl, in, in_prec, h->d_s, kp, V + J * vbytes, kp, h->d_ctrl, 1, 1, s));
+        GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1));
         // y = sum_t c_t s_t A_t s
         GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, h->d_sched, h->d_ctrl, 0.0, 1, s));
         // w = U^-T y
-        GB_LAUNCH(launch_solve(kp, ktab(h, 1), h->nl, h->d_y, kp, h->d_r, kp, nullptr, kp, h->d_ctrl, 0, 1, s));
+        GB_LAUNCH(ksolve(h, 1, h->d_y, kp, h->d_r, kp, nullptr, kp, 0, 1));
         // classical Gram-Schmidt against v_0..v_J
         GB_LAUNCH(launch_cgs_dot(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0, h->double_orth, s));
         if (J < m - 1 || h->double_orth)
@@ -383,7 +397,7 @@ gbprop_status enqueue_step(gbprop_ctx* h, void* psi) {
     GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, s));
     GB_LAUNCH(launch_combine(kp, V, N, h->d_ctrl, h->d_x, s));
     // psi <- U^-1 (beta0 V y)  (SolveSqrtOverlap(false))
-    GB_LAUNCH(launch_solve(0, &h->t64.tab[0], h->nl, h->d_x, 0, psi, kp, nullptr, 0, h->d_ctrl, 0, 0, s));
+    GB_LAUNCH(ssolve(h, 0, h->d_x, 0, psi, kp));
     GB_LAUNCH(launch_step_end(h->d_ctrl, s));
     return GBPROP_OK;
 }
@@ -447,7 +461,7 @@ gbprop_status gbprop_create(gbprop_handle* out, int nl, int nr, int precision, i
     if (nl <= 0 || nr <= 0) return fail(GBPROP_EINVAL, "nl and nr must be positive");
     if (precision != GBPROP_FP64 && precision != GBPROP_FP32_MIXED) return fail(GBPROP_EINVAL, "unknown precision");
     if (krylov_basis_size < 1 || krylov_basis_size > kMaxBasis)
-        return fail(GBPROP_EINVAL, "krylov_basis_size must be in [1, 64]");
+        return fail(GBPROP_EINVAL, "krylov_basis_size must be in [1, 45]");
     if (exponentiation_method != 0)
         return fail(GBPROP_EUNSUPPORTED, "krylov_exponentiation_method=1 (eigenvector) is not provided; use 0 (Pade)");
     gbprop_ctx* h = new gbprop_ctx();
@@ -496,7 +510,7 @@ gbprop_status gbprop_add_potential(gbprop_handle h, int storage, int npairs, con
     if (h->finalized) return fail(GBPROP_EINVAL, "handle already finalized");
     if (storage != GBPROP_STORAGE_DIAG && storage != GBPROP_STORAGE_IDENT && storage != GBPROP_STORAGE_SIMP)
         return fail(GBPROP_EUNSUPPORTED, "angular storage must be Diag, Ident or Simp");
-    if (kb < 0 || 2 * kb + 1 > 2 * h->nr + 1) return fail(GBPROP_EINVAL, "bad band half-width");
+    if (kb < 1 || kb > kMaxKd) return fail(GBPROP_EUNSUPPORTED, "radial band half-width must be in [1, 8]");
     if (h->kb >= 0 && kb != h->kb) return fail(GBPROP_EUNSUPPORTED, "all potentials must share one radial band width");
     if (!data) return fail(GBPROP_EINVAL, "null potential data");
     if (storage == GBPROP_STORAGE_DIAG && npairs != h->nl) return fail(GBPROP_EINVAL, "Diag storage needs npairs == nl");
@@ -528,9 +542,7 @@ gbprop_status gbprop_finalize(gbprop_handle h) {
     // solve tables: FP64 always (state transforms), FP32 for the mixed Krylov basis
     for (int dir = 0; dir < 2; ++dir) {
         HostSolveTab ht = build_solve_tab(h->U, h->nr, h->kd, dir);
-        if ((st = upload_solve_tab<double>(h, ht, &h->t64.tab[dir]))) return st;
-        if (h->prec == GBPROP_FP32_MIXED)
-            if ((st = upload_solve_tab<float>(h, ht, &h->t32.tab[dir]))) return st;
+        if ((st = upload_solve_tab<float>(h, ht, &h->t32.tab[dir]))) return st;
     }
     HostBandOp ho = build_band_op(h);
     if (h->prec == GBPROP_FP64) {
@@ -618,9 +630,9 @@ gbprop_status gbprop_matvec(gbprop_handle h, const void* src, void* dst, double 
     cudaStream_t s = h->stream;
     GB_CUDA(h->begin());
     if (balanced) {
-        GB_LAUNCH(launch_solve(kp, ktab(h, 0), h->nl, src, kp, h->d_s, kp, nullptr, kp, h->d_ctrl, 0, 0, s));
+        GB_LAUNCH(ksolve(h, 0, src, kp, h->d_s, kp, nullptr, kp, 0, 0));
         GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, nullptr, h->d_ctrl, scaling, 0, s));
-        GB_LAUNCH(launch_solve(kp, ktab(h, 1), h->nl, h->d_y, kp, dst, kp, nullptr, kp, h->d_ctrl, 0, 0, s));
+        GB_LAUNCH(ksolve(h, 1, h->d_y, kp, dst, kp, nullptr, kp, 0, 0));
     } else {
         GB_LAUNCH(launch_band_apply(kp, kop(h), src, dst, nullptr, h->d_ctrl, scaling, 0, s));
     }
@@ -644,7 +656,7 @@ gbprop_status gbprop_solve_sqrt_overlap(gbprop_handle h, int conj, void* psi) {
     if (!psi) return fail(GBPROP_EINVAL, "null wavefunction");
     const int kp = h->kprec();
     GB_CUDA(h->begin());
-    GB_LAUNCH(launch_solve(0, &h->t64.tab[conj ? 1 : 0], h->nl, psi, kp, psi, kp, nullptr, 0, h->d_ctrl, 0, 0, h->stream));
+    GB_LAUNCH(ssolve(h, conj ? 1 : 0, psi, kp, psi, kp));
     GB_CUDA(h->end());
     return GBPROP_OK;
 }

@@ -6,7 +6,7 @@
 
 namespace gbprop {
 
-constexpr int kMaxBasis = 64;       // largest krylov_basis_size a handle accepts
+constexpr int kMaxBasis = 45;       // largest krylov_basis_size a handle accepts (7 m*m complex in smem)
 constexpr int kWarp = 32;
 constexpr int kSolveLanes = 32;     // radial blocks per l-row in the parallel solve
 constexpr int kMaxKd = 8;           // largest band half-width of the overlap factor (order 9)
@@ -93,6 +93,11 @@ long long launch_count();
 cudaError_t launch_solve(int arith, const void* tab, int nrows, const void* in, int in_prec,
                          void* out, int out_prec, void* vstore, int v_prec, const Ctrl* ctrl,
                          int scale_mode, int check_broken, cudaStream_t s);
+// FP64-accurate solve: FP32 block solve + FP64 iterative refinement, one CTA per row.
+// tabf: SolveTab<float> of the direction; udp: (kd+1) x nr diagonals U(i, i+d) in FP64.
+cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, const void* in, int in_prec, void* out,
+                            int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
+                            cudaStream_t s);
 cudaError_t launch_band_apply(int arith, const void* op, const void* x, void* y, const SchedEntry* sched,
                               const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s);
 cudaError_t launch_tbmv(int arith, int kd, const void* ud_phys, int nl, int nr, const void* in, int in_prec,

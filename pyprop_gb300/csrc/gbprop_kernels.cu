@@ -12,6 +12,8 @@
 //     finalize in fixed order: deterministic, no atomics on values).
 #include "gbprop_internal.h"
 
+#include <cooperative_groups.h>
+
 #include <cfloat>
 #include <cmath>
 
@@ -60,21 +62,77 @@ __device__ __forceinline__ bool is_last_block(unsigned* counter) {
 
 // Sum `nvals` values over all blocks' partials (stride `pstride` doubles per
 // block) in fixed order; result into out[0..nvals).  Called by the last block.
+// Threads are split into segments per value, each summing a strided subset with
+// four independent accumulators (FP64 add latency is ~64 cycles on this part),
+// then the segments are combined in shared memory.
 __device__ void final_sum(const double* partials, int nblocks, int pstride, int nvals, double* out) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int v = warp; v < nvals; v += nw) {
-        double a = 0.0;
-        for (int b = lane; b < nblocks; b += 32) a += __ldcg(partials + (size_t)b * pstride + v);
-        a = warp_sum(a);
-        if (lane == 0) out[v] = a;
+    __shared__ double seg_sum[8][2 * kMaxBasis + 4];
+    const int S = max(1, min(8, (int)blockDim.x / max(nvals, 1)));
+    const int t = threadIdx.x;
+    if (t < S * nvals) {
+        const int v = t % nvals, sg = t / nvals;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        int b = sg;
+        for (; b + 3 * S < nblocks; b += 4 * S) {
+            a0 += __ldcg(partials + (size_t)b * pstride + v);
+            a1 += __ldcg(partials + (size_t)(b + S) * pstride + v);
+            a2 += __ldcg(partials + (size_t)(b + 2 * S) * pstride + v);
+            a3 += __ldcg(partials + (size_t)(b + 3 * S) * pstride + v);
+        }
+        for (; b < nblocks; b += S) a0 += __ldcg(partials + (size_t)b * pstride + v);
+        seg_sum[sg][v] = (a0 + a1) + (a2 + a3);
     }
     __syncthreads();
+    if (t < nvals) {
+        double a = 0.0;
+        for (int sg = 0; sg < S; ++sg) a += seg_sum[sg][t];
+        out[t] = a;
+    }
+    __syncthreads();
+}
+
+// Reduce-scatter of 16 per-lane values across a warp: after 4 butterfly levels
+// every lane holds the warp total of one value (16 adds per lane instead of 80
+// for sixteen full shuffle reductions -- the lane-wide FP64 adds are issue-bound).
+// Returns the total of value index `vidx` (valid on every lane; lanes 2k, 2k+1 agree).
+__device__ __forceinline__ double warp_reduce_scatter16(const double (&acc)[16], int lane, int& vidx) {
+    double a8[8];
+    const bool u16 = lane & 16;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const double send = u16 ? acc[j] : acc[j + 8];
+        const double keep = u16 ? acc[j + 8] : acc[j];
+        a8[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    double a4[4];
+    const bool u8 = lane & 8;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const double send = u8 ? a8[j] : a8[j + 4];
+        const double keep = u8 ? a8[j + 4] : a8[j];
+        a4[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    double a2[2];
+    const bool u4 = lane & 4;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const double send = u4 ? a4[j] : a4[j + 2];
+        const double keep = u4 ? a4[j + 2] : a4[j];
+        a2[j] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    const bool u2 = lane & 2;
+    const double send = u2 ? a2[0] : a2[1];
+    const double keep = u2 ? a2[1] : a2[0];
+    double a1 = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, 1);
+    vidx = (u16 ? 8 : 0) + (u8 ? 4 : 0) + (u4 ? 2 : 0) + (u2 ? 1 : 0);
+    return a1;
 }
 
 // Block-level sum of NV per-thread values into partials[blockIdx.x*pstride + off + k].
 template <int NV>
 __device__ void block_partials(double (&acc)[NV], int nvalid, double* partials, int pstride, int off) {
-    __shared__ double red[8][NV];
+    __shared__ double red[32][NV];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
@@ -90,37 +148,38 @@ __device__ void block_partials(double (&acc)[NV], int nvalid, double* partials, 
     __syncthreads();
 }
 
+template <>
+__device__ void block_partials<16>(double (&acc)[16], int nvalid, double* partials, int pstride, int off) {
+    __shared__ double red16[32][16];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    int vidx;
+    const double v = warp_reduce_scatter16(acc, lane, vidx);
+    if ((lane & 1) == 0) red16[warp][vidx] = v;
+    __syncthreads();
+    if (threadIdx.x < 16 && threadIdx.x < nvalid) {
+        double s0 = 0.0, s1 = 0.0;
+        int w = 0;
+        for (; w + 1 < nw; w += 2) { s0 += red16[w][threadIdx.x]; s1 += red16[w + 1][threadIdx.x]; }
+        if (w < nw) s0 += red16[w][threadIdx.x];
+        partials[(size_t)blockIdx.x * pstride + off + threadIdx.x] = s0 + s1;
+    }
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // parallel banded triangular solve (ztbsv 'U','N' / 'U','C' along r)
 // ---------------------------------------------------------------------------
 constexpr int kPitch = 33;   // smem pitch of the block-interleaved row buffer
 
-template <typename T, int KD, typename TI, typename TO, typename TV>
-__global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO* out,
-                                              TV* __restrict__ vstore, const Ctrl* __restrict__ ctrl,
-                                              int scale_mode, int check_broken) {
+// One warp solves U~ x = b for one row held in smem in block-interleaved e order
+// (element e = B*L + i at buf[i*kPitch + B]); lane B owns block B.
+//   1) local back-substitution of the block with rows pre-scaled by 1/U(e,e);
+//   2) warp-shuffle suffix scan of the kd-vector recurrence t_B = y_B[0:kd] - F_B t_{B+1};
+//   3) correction x_B -= G_B t_{B+1}.
+template <typename T, int KD>
+__device__ __forceinline__ void warp_block_solve(const SolveTab<T>& tab, cx<T>* buf, int lane) {
     using C = cx<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* buf = reinterpret_cast<C*>(smem_raw);
-    if (check_broken && ctrl->broken) return;
-    const int l = blockIdx.x, lane = threadIdx.x;
     const int n = tab.n, L = tab.L, P = tab.P;
-    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
-    const size_t base = (size_t)l * n;
-
-    for (int p = lane; p < n; p += 32) {
-        TI v = in[base + p];
-        double re = (double)v.x, im = (double)v.y;
-        if (scale_mode) { re *= sc; im *= sc; }
-        C c = mk<T>((T)re, (T)im);
-        if (vstore) vstore[base + p] = conv<TV>(c);
-        const int e = tab.dir ? (n - 1 - p) : p;
-        const int B = e / L, i = e - B * L;
-        buf[i * kPitch + B] = c;
-    }
-    __syncwarp();
-
-    // 1) local back-substitution of block B = lane (rows pre-scaled by 1/U(e,e))
     const int B = lane;
     C win[KD];
 #pragma unroll
@@ -146,8 +205,6 @@ __global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO*
         for (int d = KD - 1; d >= 1; --d) win[d] = win[d - 1];
         win[0] = x;
     }
-
-    // 2) suffix scan of the kd-vector recurrence t_B = y_B[0:kd] - F_B t_{B+1}
     C a[KD];
 #pragma unroll
     for (int c = 0; c < KD; ++c) a[c] = (B * L + c < n && B < P) ? buf[c * kPitch + B] : mk<T>(0, 0);
@@ -180,7 +237,6 @@ __global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO*
         t[c].x = __shfl_down_sync(0xffffffffu, a[c].x, 1);
         t[c].y = __shfl_down_sync(0xffffffffu, a[c].y, 1);
     }
-    // 3) correction x_B -= G_B t_{B+1}
     if (B + 1 < P) {
         for (int i = 0; i < L; ++i) {
             const int e = B * L + i;
@@ -197,11 +253,154 @@ __global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO*
         }
     }
     __syncwarp();
+}
+
+// Working-precision solve (the complex64 Krylov basis of the mixed path), one warp per row.
+template <typename T, int KD, typename TI, typename TO, typename TV>
+__global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO* out,
+                                              TV* __restrict__ vstore, const Ctrl* __restrict__ ctrl,
+                                              int scale_mode, int check_broken) {
+    using C = cx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* buf = reinterpret_cast<C*>(smem_raw);
+    if (check_broken && ctrl->broken) return;
+    const int l = blockIdx.x, lane = threadIdx.x;
+    const int n = tab.n, L = tab.L;
+    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
+    const size_t base = (size_t)l * n;
+    for (int p = lane; p < n; p += 32) {
+        TI v = in[base + p];
+        double re = (double)v.x, im = (double)v.y;
+        if (scale_mode) { re *= sc; im *= sc; }
+        C c = mk<T>((T)re, (T)im);
+        if (vstore) vstore[base + p] = conv<TV>(c);
+        const int e = tab.dir ? (n - 1 - p) : p;
+        const int B = e / L, i = e - B * L;
+        buf[i * kPitch + B] = c;
+    }
+    __syncwarp();
+    warp_block_solve<T, KD>(tab, buf, lane);
     for (int p = lane; p < n; p += 32) {
         const int e = tab.dir ? (n - 1 - p) : p;
         const int Bq = e / L, i = e - Bq * L;
         out[base + p] = conv<TO>(buf[i * kPitch + Bq]);
     }
+}
+
+// FP64-accurate solve for the FP64 path: FP32 block solve of the (power-of-two
+// scaled) residual, refined twice with FP64 residuals r = b - U~ x (mixed-precision
+// iterative refinement; the FP32 solve's relative error ~eps32*cond(U) ~ 1e-6 is
+// squared by each refinement).  One CTA per row; the FP64 work is the residual
+// band products (2*(kd+1) FMA per element per refinement), spread over the CTA.
+constexpr int kIrThreads = 256;
+constexpr int kIrRefinements = 2;
+
+template <int KD, typename TI, typename TO, typename TV>
+__global__ void __launch_bounds__(kIrThreads) k_solve_ir(SolveTab<float> tab, const double* __restrict__ udp,
+                                                         const TI* in, TO* out, TV* __restrict__ vstore,
+                                                         const Ctrl* __restrict__ ctrl, int scale_mode,
+                                                         int check_broken) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = tab.n, L = tab.L, dir = tab.dir;
+    double2* bd = reinterpret_cast<double2*>(smem_raw);
+    double2* xd = bd + n;
+    double2* rd = xd + n;
+    double* ud_s = reinterpret_cast<double*>(rd + n);                 // (KD+1) x n FP64 diagonals
+    float2* rf = reinterpret_cast<float2*>(ud_s + (size_t)(KD + 1) * n);
+    float* tsm = reinterpret_cast<float*>(rf + (size_t)L * kPitch);  // FP32 solve tables
+    __shared__ float s_red[kIrThreads / 32];
+    if (check_broken && ctrl->broken) return;
+    const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // stage the solve tables (shared by every row; L2-resident) in shared memory
+    SolveTab<float> st = tab;
+    {
+        const int nud = KD * L * 32, ninv = L * 32, ng = KD * L * 32, nm = max(tab.levels, 1) * 32 * KD * KD;
+        float* p_ud = tsm;
+        float* p_inv = p_ud + nud;
+        float* p_g = p_inv + ninv;
+        float* p_m = p_g + ng;
+        for (int k = tid; k < nud; k += kIrThreads) p_ud[k] = tab.ud[k];
+        for (int k = tid; k < ninv; k += kIrThreads) p_inv[k] = tab.invd[k];
+        for (int k = tid; k < ng; k += kIrThreads) p_g[k] = tab.g[k];
+        for (int k = tid; k < nm; k += kIrThreads) p_m[k] = tab.mlev[k];
+        for (int k = tid; k < (KD + 1) * n; k += kIrThreads) ud_s[k] = udp[k];
+        st.ud = p_ud;
+        st.invd = p_inv;
+        st.g = p_g;
+        st.mlev = p_m;
+    }
+    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
+    const size_t base = (size_t)l * n;
+    for (int p = tid; p < n; p += kIrThreads) {
+        const TI v = in[base + p];
+        double2 b = make_double2((double)v.x, (double)v.y);
+        if (scale_mode) { b.x *= sc; b.y *= sc; }
+        if (vstore) vstore[base + p] = conv<TV>(b);
+        bd[p] = b;
+        rd[p] = b;
+        xd[p] = make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    for (int it = 0; it <= kIrRefinements; ++it) {
+        if (it > 0) {
+            // r = b - U~ x in FP64 (physical coordinates)
+            for (int p = tid; p < n; p += kIrThreads) {
+                double rr = bd[p].x, ri = bd[p].y;
+                if (dir == 0) {
+#pragma unroll
+                    for (int d = 0; d <= KD; ++d) {
+                        if (p + d < n) {
+                            const double u = ud_s[(size_t)d * n + p];
+                            rr = fma(-u, xd[p + d].x, rr);
+                            ri = fma(-u, xd[p + d].y, ri);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int d = 0; d <= KD; ++d) {
+                        if (p - d >= 0) {
+                            const double u = ud_s[(size_t)d * n + p - d];
+                            rr = fma(-u, xd[p - d].x, rr);
+                            ri = fma(-u, xd[p - d].y, ri);
+                        }
+                    }
+                }
+                rd[p] = make_double2(rr, ri);
+            }
+            __syncthreads();
+        }
+        // power-of-two scale so that the FP32 right-hand side is O(1)
+        float mx = 0.f;
+        for (int p = tid; p < n; p += kIrThreads) mx = fmaxf(mx, fmaxf(fabsf((float)rd[p].x), fabsf((float)rd[p].y)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) s_red[warp] = mx;
+        __syncthreads();
+        mx = 0.f;
+#pragma unroll
+        for (int w = 0; w < kIrThreads / 32; ++w) mx = fmaxf(mx, s_red[w]);
+        if (mx == 0.f) break;                       // exact solution reached (or zero rhs)
+        int ex;
+        frexpf(mx, &ex);
+        const double scale = ldexp(1.0, -ex), unscale = ldexp(1.0, ex);
+        for (int p = tid; p < n; p += kIrThreads) {
+            const int e = dir ? (n - 1 - p) : p;
+            const int B = e / L, i = e - B * L;
+            rf[i * kPitch + B] = make_float2((float)(rd[p].x * scale), (float)(rd[p].y * scale));
+        }
+        __syncthreads();
+        if (warp == 0) warp_block_solve<float, KD>(st, rf, lane);
+        __syncthreads();
+        for (int p = tid; p < n; p += kIrThreads) {
+            const int e = dir ? (n - 1 - p) : p;
+            const int B = e / L, i = e - B * L;
+            const float2 dlt = rf[i * kPitch + B];
+            xd[p].x += (double)dlt.x * unscale;
+            xd[p].y += (double)dlt.y * unscale;
+        }
+        __syncthreads();
+    }
+    for (int p = tid; p < n; p += kIrThreads) out[base + p] = conv<TO>(xd[p]);
 }
 
 template <typename T, int KD>
@@ -257,70 +456,147 @@ cudaError_t launch_solve(int arith, const void* tab, int nrows, const void* in, 
                           scale_mode, check_broken, s);
 }
 
+template <int KD>
+static cudaError_t solve_ir_kd(const SolveTab<float>& tab, const double* udp, int nrows, const void* in, int in_prec,
+                               void* out, int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode,
+                               int check_broken, cudaStream_t s) {
+    const size_t tabf = (size_t)KD * tab.L * 32 * 2 + (size_t)tab.L * 32 + (size_t)(tab.levels > 0 ? tab.levels : 1) * 32 * KD * KD;
+    const size_t smem = (size_t)3 * tab.n * sizeof(double2) + (size_t)(KD + 1) * tab.n * sizeof(double) +
+                        (size_t)tab.L * kPitch * sizeof(float2) + tabf * sizeof(float);
+    dim3 grid(nrows), block(kIrThreads);
+#define GB_IR_CASE(TI_, TO_, TV_)                                                                                \
+    {                                                                                                            \
+        auto kern = k_solve_ir<KD, TI_, TO_, TV_>;                                                               \
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        kern<<<grid, block, smem, s>>>(tab, udp, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,      \
+                                       check_broken);                                                            \
+        return cudaGetLastError();                                                                               \
+    }
+    const int key = in_prec * 4 + out_prec * 2 + v_prec;
+    switch (key) {
+        case 0: GB_IR_CASE(double2, double2, double2)
+        case 1: GB_IR_CASE(double2, double2, float2)
+        case 2: GB_IR_CASE(double2, float2, double2)
+        case 3: GB_IR_CASE(double2, float2, float2)
+        case 4: GB_IR_CASE(float2, double2, double2)
+        case 5: GB_IR_CASE(float2, double2, float2)
+        case 6: GB_IR_CASE(float2, float2, double2)
+        default: GB_IR_CASE(float2, float2, float2)
+    }
+#undef GB_IR_CASE
+}
+
+cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, const void* in, int in_prec, void* out,
+                            int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
+                            cudaStream_t s) {
+    count_launch();
+    const SolveTab<float>& tab = *(const SolveTab<float>*)tabf;
+    switch (tab.kd) {
+#define GB_KD(K) \
+    case K: return solve_ir_kd<K>(tab, udp, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, scale_mode, check_broken, s);
+        GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
+#undef GB_KD
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // tensor-potential matvec over the term list (TensorPotentialMultiply_*_BandNH)
 // ---------------------------------------------------------------------------
-constexpr int kBandTile = 128;
+constexpr int kBandThreads = 128;
+constexpr int kBandPer = 2;                          // radial elements per thread (i, i + 128)
+constexpr int kBandTile = kBandThreads * kBandPer;   // radial elements per block
 
-template <typename T>
-__global__ void __launch_bounds__(kBandTile) k_band_apply(BandOp<T> op, const cx<T>* __restrict__ x,
-                                                          cx<T>* __restrict__ y, const SchedEntry* __restrict__ sched,
-                                                          const Ctrl* __restrict__ ctrl, double scal_val,
-                                                          int check_broken) {
+// One block: destination row l = blockIdx.y, radial tile blockIdx.x.  For every term
+// of row l the source row's tile (with a kb halo) is staged in shared memory; each
+// thread accumulates two elements with the band sum split into even/odd diagonals
+// (eight independent FMA chains per thread to cover the FP64 latency).
+template <typename T, int KB>
+__global__ void __launch_bounds__(kBandThreads) k_band_apply(BandOp<T> op, const cx<T>* __restrict__ x,
+                                                             cx<T>* __restrict__ y, const SchedEntry* __restrict__ sched,
+                                                             const Ctrl* __restrict__ ctrl, double scal_val,
+                                                             int check_broken) {
     using C = cx<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* sx = reinterpret_cast<C*>(smem_raw);
+    constexpr int W = 2 * KB + 1;
+    __shared__ C sx[kBandTile + 2 * KB];
     if (check_broken && ctrl->broken) return;
-    const int l = blockIdx.y, i0 = blockIdx.x * kBandTile, tid = threadIdx.x, i = i0 + tid;
-    const int nr = op.nr, kb = op.kb, W = 2 * kb + 1;
+    const int l = blockIdx.y, i0 = blockIdx.x * kBandTile, tid = threadIdx.x;
+    const int nr = op.nr;
     const double scal = sched ? sched[ctrl->step].scaling : scal_val;
-    T yr = 0, yi = 0;
+    T yr[kBandPer], yi[kBandPer];
+#pragma unroll
+    for (int e = 0; e < kBandPer; ++e) { yr[e] = 0; yi[e] = 0; }
     const int t0 = op.row_ptr[l], t1 = op.row_ptr[l + 1];
     for (int t = t0; t < t1; ++t) {
-        const int src = op.t_src[t];
-        const size_t sbase = (size_t)src * nr;
+        const size_t sbase = (size_t)op.t_src[t] * nr;
         __syncthreads();
-        for (int j = tid; j < kBandTile + 2 * kb; j += kBandTile) {
-            const int g = i0 - kb + j;
+        for (int j = tid; j < kBandTile + 2 * KB; j += kBandThreads) {
+            const int g = i0 - KB + j;
             sx[j] = (g >= 0 && g < nr) ? x[sbase + g] : mk<T>(0, 0);
         }
         __syncthreads();
-        if (i < nr) {
-            const T* A = op.slots + (size_t)op.t_slot[t] * W * nr + i;
-            T ar = 0, ai = 0;
-            for (int d = 0; d < W; ++d) {
-                const T a = __ldg(A + (size_t)d * nr);
-                const C v = sx[tid + d];
-                ar = fma(a, v.x, ar);
-                ai = fma(a, v.y, ai);
+        const T* A = op.slots + (size_t)op.t_slot[t] * W * nr;
+        double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
+        if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
+        const T Cr = (T)cr, Ci = (T)ci;
+#pragma unroll
+        for (int e = 0; e < kBandPer; ++e) {
+            const int li = tid + e * kBandThreads;
+            const int i = i0 + li;
+            if (i < nr) {
+                T a[W];
+#pragma unroll
+                for (int d = 0; d < W; ++d) a[d] = __ldg(A + (size_t)d * nr + i);
+                T ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
+#pragma unroll
+                for (int d = 0; d < W; d += 2) {
+                    const C v = sx[li + d];
+                    ar0 = fma(a[d], v.x, ar0);
+                    ai0 = fma(a[d], v.y, ai0);
+                }
+#pragma unroll
+                for (int d = 1; d < W; d += 2) {
+                    const C v = sx[li + d];
+                    ar1 = fma(a[d], v.x, ar1);
+                    ai1 = fma(a[d], v.y, ai1);
+                }
+                const T ar = ar0 + ar1, ai = ai0 + ai1;
+                yr[e] += Cr * ar - Ci * ai;
+                yi[e] += Cr * ai + Ci * ar;
             }
-            double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
-            if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
-            const T Cr = (T)cr, Ci = (T)ci;
-            yr += Cr * ar - Ci * ai;
-            yi += Cr * ai + Ci * ar;
         }
     }
-    if (i < nr) y[(size_t)l * nr + i] = mk<T>(yr, yi);
+#pragma unroll
+    for (int e = 0; e < kBandPer; ++e) {
+        const int i = i0 + tid + e * kBandThreads;
+        if (i < nr) y[(size_t)l * nr + i] = mk<T>(yr[e], yi[e]);
+    }
+}
+
+template <typename T, int KB>
+static void band_apply_kb(const BandOp<T>& op, const void* x, void* y, const SchedEntry* sched, const Ctrl* ctrl,
+                          double scaling, int check_broken, cudaStream_t s) {
+    dim3 grid((op.nr + kBandTile - 1) / kBandTile, op.nl);
+    k_band_apply<T, KB><<<grid, kBandThreads, 0, s>>>(op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl, scaling, check_broken);
+}
+
+template <typename T>
+static cudaError_t band_apply_dispatch(const BandOp<T>& op, const void* x, void* y, const SchedEntry* sched,
+                                       const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s) {
+    switch (op.kb) {
+#define GB_KB(K) case K: band_apply_kb<T, K>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
+        GB_KB(1) GB_KB(2) GB_KB(3) GB_KB(4) GB_KB(5) GB_KB(6) GB_KB(7) GB_KB(8)
+#undef GB_KB
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_band_apply(int arith, const void* opv, const void* x, void* y, const SchedEntry* sched,
                               const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s) {
     count_launch();
-    if (arith == 0) {
-        const BandOp<double>& op = *(const BandOp<double>*)opv;
-        dim3 grid((op.nr + kBandTile - 1) / kBandTile, op.nl);
-        size_t smem = (kBandTile + 2 * op.kb) * sizeof(double2);
-        k_band_apply<double><<<grid, kBandTile, smem, s>>>(op, (const double2*)x, (double2*)y, sched, ctrl, scaling,
-                                                           check_broken);
-    } else {
-        const BandOp<float>& op = *(const BandOp<float>*)opv;
-        dim3 grid((op.nr + kBandTile - 1) / kBandTile, op.nl);
-        size_t smem = (kBandTile + 2 * op.kb) * sizeof(float2);
-        k_band_apply<float><<<grid, kBandTile, smem, s>>>(op, (const float2*)x, (float2*)y, sched, ctrl, scaling,
-                                                          check_broken);
-    }
-    return cudaGetLastError();
+    if (arith == 0) return band_apply_dispatch(*(const BandOp<double>*)opv, x, y, sched, ctrl, scaling, check_broken, s);
+    return band_apply_dispatch(*(const BandOp<float>*)opv, x, y, sched, ctrl, scaling, check_broken, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -368,11 +644,11 @@ cudaError_t launch_tbmv(int arith, int kd, const void* ud, int nl, int nr, const
 // ---------------------------------------------------------------------------
 // reductions: ||x||, Gram-Schmidt projections and updates
 // ---------------------------------------------------------------------------
-constexpr int kRedThreads = 256;
+constexpr int kRedThreads = 512;
 constexpr int kPStride = 2 * kMaxBasis + 4;   // doubles of partials per block
 constexpr int kKChunk = 8;                    // basis vectors handled per pass over w
 
-int grid_reduce_blocks() { return 152 * 2; }
+int grid_reduce_blocks() { return 152; }
 
 template <typename CI>
 __global__ void __launch_bounds__(kRedThreads) k_norm(const CI* __restrict__ x, long n, double* partials,
@@ -424,15 +700,17 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_dot(const cx<T>* __restrict
         for (int k = 0; k < 2 * kKChunk; ++k) acc[k] = 0.0;
         for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
             const C wi = w[i];
-            // products in the working precision, promoted per element
+            const double wr = (double)wi.x, wim = (double)wi.y;
+            // conj(v) * w, each product exact in FP64 for complex64 operands
 #pragma unroll
             for (int k = 0; k < kKChunk; ++k) {
                 if (kc + k < nv) {
                     const C v = V[(size_t)(kc + k) * n + i];
-                    const T pr = v.x * wi.x + v.y * wi.y;
-                    const T pi = v.x * wi.y - v.y * wi.x;
-                    acc[2 * k] += (double)pr;
-                    acc[2 * k + 1] += (double)pi;
+                    const double vr = (double)v.x, vi = (double)v.y;
+                    acc[2 * k] = fma(vr, wr, acc[2 * k]);
+                    acc[2 * k] = fma(vi, wim, acc[2 * k]);
+                    acc[2 * k + 1] = fma(vr, wim, acc[2 * k + 1]);
+                    acc[2 * k + 1] = fma(-vi, wr, acc[2 * k + 1]);
                 }
             }
         }
@@ -495,18 +773,33 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_update(const cx<T>* __restr
     __syncthreads();
     double acc[1] = {0.0};
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        T sr = 0, si = 0;
-        for (int k = 0; k < nv; ++k) {
-            const C v = V[(size_t)k * n + i];
-            const C hk = hs[k];
-            sr = fma(v.x, hk.x, sr);
-            sr = fma(-v.y, hk.y, sr);
-            si = fma(v.x, hk.y, si);
-            si = fma(v.y, hk.x, si);
+        // four independent accumulation chains (FP64 FMA latency ~64 cycles)
+        T sr0 = 0, si0 = 0, sr1 = 0, si1 = 0;
+        int k = 0;
+        for (; k + 1 < nv; k += 2) {
+            const C v0 = V[(size_t)k * n + i];
+            const C v1 = V[(size_t)(k + 1) * n + i];
+            const C h0 = hs[k], h1 = hs[k + 1];
+            sr0 = fma(v0.x, h0.x, sr0);
+            sr0 = fma(-v0.y, h0.y, sr0);
+            si0 = fma(v0.x, h0.y, si0);
+            si0 = fma(v0.y, h0.x, si0);
+            sr1 = fma(v1.x, h1.x, sr1);
+            sr1 = fma(-v1.y, h1.y, sr1);
+            si1 = fma(v1.x, h1.y, si1);
+            si1 = fma(v1.y, h1.x, si1);
+        }
+        if (k < nv) {
+            const C v0 = V[(size_t)k * n + i];
+            const C h0 = hs[k];
+            sr0 = fma(v0.x, h0.x, sr0);
+            sr0 = fma(-v0.y, h0.y, sr0);
+            si0 = fma(v0.x, h0.y, si0);
+            si0 = fma(v0.y, h0.x, si0);
         }
         C r = w[i];
-        r.x -= sr;
-        r.y -= si;
+        r.x -= sr0 + sr1;
+        r.y -= si0 + si1;
         w[i] = r;
         const double re = (double)r.x, im = (double)r.y;
         acc[0] = fma(re, re, acc[0]);
@@ -833,8 +1126,368 @@ __global__ void __launch_bounds__(256) k_expm(Ctrl* ctrl, double* Hg, int m, con
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Cluster version of the Hessenberg exponential: the same scaling-and-squaring
+// Pade (order 6) as k_expm, with every m x m product split by rows over the CL
+// CTAs of a thread-block cluster.  Each CTA keeps full copies of the matrices in
+// its shared memory; a product's rows are computed by their owner CTA (row % CL)
+// and stored into every CTA's copy through distributed shared memory, followed by
+// a cluster barrier.  The LU factorisation of Q-P runs redundantly in every CTA
+// (identical arithmetic, so identical results); the m right-hand sides of the
+// solve are split over the CTAs by column.  FP64 throughput is ~2 FMA/clk/SM on
+// GB300, so spreading the products over CL SMs is what makes this step cheap.
+// ---------------------------------------------------------------------------
+namespace cg = cooperative_groups;
+
+template <int CL>
+__device__ void cl_matmul(cg::cluster_group& cl, int rank, int m, const double2* A, const double2* B, double2* Cdst) {
+    constexpr int KS = 4;                                // threads per output entry (split over k)
+    const int mine = (m - rank + CL - 1) / CL;           // rows r = rank, rank + CL, ...
+    const int total = mine * m * KS;
+    for (int base = 0; base < total; base += blockDim.x) {
+        const int idx = base + threadIdx.x;
+        const bool act = idx < total;
+        const int o = idx / KS, ks = idx % KS;
+        const int r = rank + (o / m) * CL, c = o % m;
+        double arA = 0.0, arB = 0.0, aiA = 0.0, aiB = 0.0;
+        if (act)
+            for (int k = ks; k < m; k += KS) {
+                const double2 a = A[r * m + k], b = B[k * m + c];
+                arA = fma(a.x, b.x, arA);
+                arB = fma(a.y, b.y, arB);
+                aiA = fma(a.x, b.y, aiA);
+                aiB = fma(a.y, b.x, aiB);
+            }
+        double sr = arA - arB, si = aiA + aiB;
+        sr += __shfl_xor_sync(0xffffffffu, sr, 1);
+        si += __shfl_xor_sync(0xffffffffu, si, 1);
+        sr += __shfl_xor_sync(0xffffffffu, sr, 2);
+        si += __shfl_xor_sync(0xffffffffu, si, 2);
+        if (act && ks == 0) {
+            const double2 v = make_double2(sr, si);
+#pragma unroll
+            for (int q = 0; q < CL; ++q) {
+                double2* dst = cl.map_shared_rank(Cdst, q);
+                dst[r * m + c] = v;
+            }
+        }
+    }
+    cl.sync();
+}
+
+template <int CL>
+__global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, int m, const SchedEntry* sched) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int mm = m * m;
+    double2* buf[7];
+    for (int k = 0; k < 7; ++k) buf[k] = reinterpret_cast<double2*>(smem_raw) + (size_t)k * mm;
+    double2* A = buf[0];
+    double2* A2 = buf[1];
+    double2* P = buf[2];
+    double2* Q = buf[3];
+    double2* T = buf[4];
+    double2* LU = buf[5];
+    double2* X = buf[6];
+    __shared__ double red[8];
+    __shared__ int piv[kMaxBasis];
+    __shared__ int s_p;
+    __shared__ int s_info;
+    __shared__ double s_c[8];
+    const int tid = threadIdx.x;
+    const SchedEntry se = sched[ctrl->step];
+    const double2 f = make_double2(se.dt_im, -se.dt_re);   // -i * dt (pamp.h:634)
+    double mx = 0.0;
+    for (int k = tid; k < mm; k += blockDim.x) {
+        const double2 a = cmulz(make_double2(Hg[2 * k], Hg[2 * k + 1]), f);
+        A[k] = a;
+        mx = fmax(mx, hypot(a.x, a.y));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) red[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, red[w]);
+        int sord = v > 0.0 ? (int)ceil(log2(v)) : 0;
+        if (sord < 0) sord = 0;
+        s_p = sord;
+        s_info = 0;
+        const int order = 6;
+        s_c[0] = 1.0;
+        for (int i = 0; i < order; ++i) s_c[i + 1] = s_c[i] * (double)(order - i) / (double)((i + 1) * (2 * order - i));
+    }
+    __syncthreads();
+    const int sorder = s_p;
+    const double sc = pow(2.0, (double)sorder);
+    for (int k = tid; k < mm; k += blockDim.x) { A[k].x /= sc; A[k].y /= sc; }
+    // every CTA scaled its own copy of A: barrier before anyone writes remotely
+    cl.sync();
+    if (rank == 0)
+        for (int k = tid; k < mm; k += blockDim.x) {
+            const double2 a = cmulz(make_double2(Hg[2 * k], Hg[2 * k + 1]), f);
+            Hg[2 * k] = a.x;
+            Hg[2 * k + 1] = a.y;
+        }
+    cl_matmul<CL>(cl, rank, m, A, A, A2);
+    // Horner in A^2 (pamp.h:497-539); first factors are scalar multiples of I
+    for (int k = tid; k < mm; k += blockDim.x) {
+        Q[k] = make_double2(s_c[6] * A2[k].x, s_c[6] * A2[k].y);
+        P[k] = make_double2(s_c[5] * A2[k].x, s_c[5] * A2[k].y);
+    }
+    __syncthreads();
+    for (int r = tid; r < m; r += blockDim.x) { Q[r * m + r].x += s_c[4]; P[r * m + r].x += s_c[3]; }
+    __syncthreads();
+    cl_matmul<CL>(cl, rank, m, Q, A2, T);                  // i = 2
+    { double2* t = Q; Q = T; T = t; }
+    for (int r = tid; r < m; r += blockDim.x) Q[r * m + r].x += s_c[2];
+    __syncthreads();
+    cl_matmul<CL>(cl, rank, m, P, A2, T);                  // i = 1
+    { double2* t = P; P = T; T = t; }
+    for (int r = tid; r < m; r += blockDim.x) P[r * m + r].x += s_c[1];
+    __syncthreads();
+    cl_matmul<CL>(cl, rank, m, Q, A2, T);                  // i = 0
+    { double2* t = Q; Q = T; T = t; }
+    for (int r = tid; r < m; r += blockDim.x) Q[r * m + r].x += s_c[0];
+    __syncthreads();
+    cl_matmul<CL>(cl, rank, m, P, A, T);                   // P = P A
+    { double2* t = P; P = T; T = t; }
+    // X = (Q - P)^-1 P (pamp.h:541-556).  D = Q - P is the Pade denominator, well
+    // conditioned after scaling; it is inverted approximately in FP32 (LU with
+    // partial pivoting, then the m unit right-hand sides), and X is refined twice
+    // with FP64 residuals R = P - D X.  Each refinement squares the FP32 error
+    // (~1e-6), so X is FP64-accurate; only the FP64 residual products are
+    // throughput-heavy and they are split over the cluster by column.
+    for (int k = tid; k < mm; k += blockDim.x) LU[k] = make_double2(Q[k].x - P[k].x, Q[k].y - P[k].y);   // D (FP64)
+    float2* F = reinterpret_cast<float2*>(X);            // FP32 LU of D      (m*m float2)
+    float2* Z = F + mm;                                  // FP32 inverse of D (m*m float2)
+    for (int k = tid; k < mm; k += blockDim.x) F[k] = make_float2((float)LU[k].x, (float)LU[k].y);
+    __syncthreads();
+    for (int k = 0; k < m; ++k) {
+        if (tid < 32) {
+            float best = -1.f;
+            int bi = k;
+            for (int r = k + tid; r < m; r += 32) {
+                const float v = fabsf(F[r * m + k].x) + fabsf(F[r * m + k].y);
+                if (v > best) { best = v; bi = r; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (tid == 0) {
+                piv[k] = bi;
+                if (best == 0.f && !s_info) s_info = k + 1;
+                s_p = (best == 0.f) ? -1 : bi;
+            }
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p >= 0) {
+            if (p != k)
+                for (int c = tid; c < m; c += blockDim.x) {
+                    const float2 t = F[k * m + c];
+                    F[k * m + c] = F[p * m + c];
+                    F[p * m + c] = t;
+                }
+            __syncthreads();
+            const float2 d = F[k * m + k];
+            const float den = d.x * d.x + d.y * d.y;
+            const float2 inv = make_float2(d.x / den, -d.y / den);
+            for (int r = k + 1 + tid; r < m; r += blockDim.x) {
+                const float2 a = F[r * m + k];
+                F[r * m + k] = make_float2(a.x * inv.x - a.y * inv.y, a.x * inv.y + a.y * inv.x);
+            }
+            __syncthreads();
+            const int rem = m - k - 1;
+            for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
+                const int r = k + 1 + idx / rem, c = k + 1 + idx % rem;
+                const float2 fr = F[r * m + k], u = F[k * m + c];
+                float2 q = F[r * m + c];
+                q.x -= fr.x * u.x - fr.y * u.y;
+                q.y -= fr.x * u.y + fr.y * u.x;
+                F[r * m + c] = q;
+            }
+        }
+        __syncthreads();
+    }
+    const int info = s_info;
+    if (info) {
+        if (rank == 0 && tid == 0) ctrl->lu_info = info;
+    } else {
+        // Z = D^-1 in FP32: thread c solves L U z = P_perm e_c
+        for (int c = tid; c < m; c += blockDim.x) {
+            float2 z[kMaxBasis];
+            for (int r = 0; r < m; ++r) z[r] = make_float2(0.f, 0.f);
+            z[c] = make_float2(1.f, 0.f);
+            for (int k = 0; k < m; ++k) {          // row interchanges in order
+                const int pk = piv[k];
+                if (pk != k) { const float2 t = z[k]; z[k] = z[pk]; z[pk] = t; }
+            }
+            for (int r = 0; r < m; ++r) {
+                float2 a = z[r];
+                for (int k = 0; k < r; ++k) {
+                    const float2 l = F[r * m + k];
+                    a.x -= l.x * z[k].x - l.y * z[k].y;
+                    a.y -= l.x * z[k].y + l.y * z[k].x;
+                }
+                z[r] = a;
+            }
+            for (int r = m - 1; r >= 0; --r) {
+                float2 a = z[r];
+                for (int k = r + 1; k < m; ++k) {
+                    const float2 u = F[r * m + k];
+                    a.x -= u.x * z[k].x - u.y * z[k].y;
+                    a.y -= u.x * z[k].y + u.y * z[k].x;
+                }
+                const float2 d = F[r * m + r];
+                const float den = d.x * d.x + d.y * d.y;
+                z[r] = make_float2((a.x * d.x + a.y * d.y) / den, (a.y * d.x - a.x * d.y) / den);
+            }
+            for (int r = 0; r < m; ++r) Z[r * m + c] = z[r];
+        }
+        __syncthreads();
+        // this CTA's columns c = rank + j*CL of X (FP64, kept in T), residual R in Q's buffer
+        const int ncol = (m - rank + CL - 1) / CL;
+        double2* Xc = T;
+        double2* R = Q;
+        for (int it = 0; it < 3; ++it) {
+            // R = P - D X  (it == 0: R = P, X = 0)
+            for (int idx = tid; idx < ncol * m; idx += blockDim.x) {
+                const int c = rank + (idx / m) * CL, r = idx % m;
+                double rr = P[r * m + c].x, ri = P[r * m + c].y;
+                if (it > 0)
+                    for (int k = 0; k < m; ++k) {
+                        const double2 d = LU[r * m + k], x = Xc[k * m + c];
+                        rr = fma(-d.x, x.x, rr);
+                        rr = fma(d.y, x.y, rr);
+                        ri = fma(-d.x, x.y, ri);
+                        ri = fma(-d.y, x.x, ri);
+                    }
+                R[r * m + c] = make_double2(rr, ri);
+            }
+            __syncthreads();
+            // X += Z R  (FP32 products on the FP32-rounded residual; FP64 update)
+            for (int idx = tid; idx < ncol * m; idx += blockDim.x) {
+                const int c = rank + (idx / m) * CL, r = idx % m;
+                float ar = 0.f, ai = 0.f;
+                for (int k = 0; k < m; ++k) {
+                    const float2 zz = Z[r * m + k];
+                    const float xr = (float)R[k * m + c].x, xi = (float)R[k * m + c].y;
+                    ar = fmaf(zz.x, xr, ar);
+                    ar = fmaf(-zz.y, xi, ar);
+                    ai = fmaf(zz.x, xi, ai);
+                    ai = fmaf(zz.y, xr, ai);
+                }
+                if (it == 0) Xc[r * m + c] = make_double2((double)ar, (double)ai);
+                else { Xc[r * m + c].x += (double)ar; Xc[r * m + c].y += (double)ai; }
+            }
+            __syncthreads();
+        }
+        // E = I + 2 X for this CTA's columns, broadcast into every CTA's A2 buffer
+        for (int idx = tid; idx < ncol * m; idx += blockDim.x) {
+            const int c = rank + (idx / m) * CL, r = idx % m;
+            double2 v = make_double2(2.0 * Xc[r * m + c].x, 2.0 * Xc[r * m + c].y);
+            if (r == c) v.x += 1.0;
+#pragma unroll
+            for (int q = 0; q < CL; ++q) {
+                double2* dst = cl.map_shared_rank(A2, q);
+                dst[r * m + c] = v;
+            }
+        }
+    }
+    cl.sync();
+    { double2* t = A; A = A2; A2 = t; }
+    if (!info) {
+        for (int i = 0; i < sorder; ++i) {
+            cl_matmul<CL>(cl, rank, m, A, A, T);
+            double2* t = A; A = T; T = t;
+        }
+        if (rank == 0) {
+            for (int k = tid; k < m; k += blockDim.x) {
+                ctrl->y[2 * k] = A[k * m].x;
+                ctrl->y[2 * k + 1] = A[k * m].y;
+            }
+            if (tid == 0) {
+                const double2 yl = A[(m - 1) * m];
+                ctrl->err_est = yl.x * yl.x + yl.y * yl.y;
+                ctrl->scaling_order = sorder;
+            }
+        }
+    }
+    // no CTA may exit while others can still address its shared memory
+    cl.sync();
+}
+
+static int g_expm_cluster[kMaxBasis + 1];   // per basis size: 0 unknown, 1 single CTA, else cluster size
+
+template <int CL>
+static cudaError_t launch_expm_cl(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s) {
+    const size_t smem = (size_t)7 * m * m * sizeof(double2);
+    auto kern = k_expm_cluster<CL>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (CL > 8) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CL);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, ctrl, H, m, sched);
+}
+
+template <int CL>
+static bool cluster_fits(int m) {
+    const size_t smem = (size_t)7 * m * m * sizeof(double2);
+    auto kern = k_expm_cluster<CL>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return false;
+    if (CL > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        return false;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CL);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    cudaError_t e = cudaOccupancyMaxActiveClusters(&n, kern, &cfg);
+    cudaGetLastError();
+    return e == cudaSuccess && n > 0;
+}
+
+int expm_cluster_size(int m) {
+    if (m < 1 || m > kMaxBasis) return 0;
+    if (g_expm_cluster[m] == 0) {
+        if (cluster_fits<16>(m)) g_expm_cluster[m] = 16;
+        else if (cluster_fits<8>(m)) g_expm_cluster[m] = 8;
+        else g_expm_cluster[m] = 1;
+    }
+    return g_expm_cluster[m] == 1 ? 0 : g_expm_cluster[m];
+}
+
 cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s) {
     count_launch();
+    const int cl = expm_cluster_size(m);
+    if (cl == 16) return launch_expm_cl<16>(ctrl, H, m, sched, s);
+    if (cl == 8) return launch_expm_cl<8>(ctrl, H, m, sched, s);
     const size_t smem = (size_t)5 * m * m * sizeof(double2);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_expm<<<1, 256, smem, s>>>(ctrl, H, m, sched);
