@@ -22,6 +22,8 @@
 #ifndef GBPROP_H
 #define GBPROP_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -144,6 +146,18 @@ gbprop_status gbprop_synchronize(gbprop_handle h);
 gbprop_status gbprop_tensor_multiply_bandnh(int storage, const void* V, int npairs, const int* pairs,
                                             int kb, double scaling, const void* src, void* dst,
                                             int nl, int nr, void* stream);
+
+/* Stateless block inner product of the Arnoldi step: BLASIntegrationFunctor::InnerProduct
+ * (core/krylov/piram/piram/functors.h:236-240, zgemv 'C' over the first nv Krylov vectors):
+ *   out[2k], out[2k+1] = Re, Im of sum_i conj(V[k][i]) * w[i],  k < nv
+ * and, when want_norm != 0, out[2nv] = sum_i |w[i]|^2.  V is nv rows of n elements
+ * (row stride n), all DEVICE pointers of the given precision (GBPROP_FP64: complex128,
+ * GBPROP_FP32_MIXED: complex64; sums are accumulated in FP64 either way).  workspace is
+ * caller-owned DEVICE scratch of at least gbprop_block_inner_product_workspace(n, nv)
+ * bytes -- the role of the reference's `temp` argument.  Deterministic summation order. */
+size_t gbprop_block_inner_product_workspace(long n, int nv);
+gbprop_status gbprop_block_inner_product(int precision, const void* V, long n, int nv, const void* w, int want_norm,
+                                         double* out, void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -558,7 +558,7 @@ gbprop_status gbprop_finalize(gbprop_handle h) {
     GB_CUDA(cudaMemsetAsync(h->d_ctrl, 0, sizeof(Ctrl), h->stream));
     if ((st = h->dalloc(&h->d_H, (size_t)2 * h->m * h->m * sizeof(double)))) return st;
     GB_CUDA(cudaMemsetAsync(h->d_H, 0, (size_t)2 * h->m * h->m * sizeof(double), h->stream));
-    if ((st = h->dalloc(&h->d_partials, (size_t)grid_reduce_blocks() * (2 * kMaxBasis + 4) * sizeof(double)))) return st;
+    if ((st = h->dalloc(&h->d_partials, partials_capacity() * sizeof(double)))) return st;
     if ((st = h->dalloc(&h->d_counter, 64))) return st;
     GB_CUDA(cudaMemsetAsync(h->d_counter, 0, 64, h->stream));
     const size_t ke = h->kelem();
@@ -711,6 +711,33 @@ gbprop_status gbprop_tensor_multiply_bandnh(int storage, const void* V, int npai
     if (nl <= 0 || nr <= 0 || kb < 0) return fail(GBPROP_EINVAL, "bad sizes");
     GB_LAUNCH(launch_tensor_multiply_ref(storage == GBPROP_STORAGE_DIAG ? 0 : 1, (const double2*)V, npairs, pairs, kb,
                                          scaling, (const double2*)src, (double2*)dst, nl, nr, (cudaStream_t)stream));
+    return GBPROP_OK;
+}
+
+size_t gbprop_block_inner_product_workspace(long n, int nv) {
+    if (n <= 0 || nv < 1 || nv > kMaxBasis) return 0;
+    // partial sums (the launch shape depends on whether ||w||^2 is requested: size for
+    // the larger of the two), then one 256-byte aligned counter word
+    const size_t a = block_inner_scratch_doubles(n, nv), b = block_inner_scratch_doubles(n, nv + 1);
+    const size_t sums = (a > b ? a : b) * sizeof(double);
+    return ((sums + 255) / 256) * 256 + 256;
+}
+
+gbprop_status gbprop_block_inner_product(int precision, const void* V, long n, int nv, const void* w, int want_norm,
+                                         double* out, void* workspace, size_t workspace_bytes, void* stream) {
+    if (precision != GBPROP_FP64 && precision != GBPROP_FP32_MIXED) return fail(GBPROP_EINVAL, "unknown precision");
+    if (n <= 0 || nv < 1 || nv > kMaxBasis) return fail(GBPROP_EINVAL, "need n > 0 and 1 <= nv <= 45");
+    if (!V || !w || !out || !workspace) return fail(GBPROP_EINVAL, "null buffer");
+    const size_t need = gbprop_block_inner_product_workspace(n, nv);
+    if (workspace_bytes < need)
+        return fail(GBPROP_EINVAL, "workspace too small: need " + std::to_string(need) + " bytes");
+    const size_t sums = need - 256;
+    double* partials = (double*)workspace;
+    unsigned* counter = (unsigned*)((char*)workspace + sums);
+    cudaStream_t s = (cudaStream_t)stream;
+    GB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), s));
+    GB_LAUNCH(launch_block_inner(precision == GBPROP_FP64 ? 0 : 1, V, n, nv, w, want_norm ? 1 : 0, out, partials,
+                                 counter, s));
     return GBPROP_OK;
 }
 

@@ -106,6 +106,10 @@ cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsig
                         cudaStream_t s);
 cudaError_t launch_cgs_dot(int prec, const void* V, long n, int nv, const void* w, double* partials,
                            unsigned* counter, Ctrl* ctrl, int mode, int want_norm, cudaStream_t s);
+// Stateless block inner product into a caller buffer (out: 2nv doubles, + ||w||^2 when want_norm).
+size_t block_inner_scratch_doubles(long n, int nvals);
+cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const void* w, int want_norm, double* out,
+                               double* partials, unsigned* counter, cudaStream_t s);
 cudaError_t launch_cgs_update(int prec, const void* V, long n, int nv, void* w, double* partials,
                               unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
 cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, cudaStream_t s);
@@ -119,5 +123,6 @@ cudaError_t launch_tensor_multiply_ref(int storage, const double2* V, int npairs
 cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s);
 
 int grid_reduce_blocks();
+size_t partials_capacity();
 
 }  // namespace gbprop

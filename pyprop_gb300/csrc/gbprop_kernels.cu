@@ -288,12 +288,13 @@ __global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO*
 }
 
 // FP64-accurate solve for the FP64 path: FP32 block solve of the (power-of-two
-// scaled) residual, refined twice with FP64 residuals r = b - U~ x (mixed-precision
-// iterative refinement; the FP32 solve's relative error ~eps32*cond(U) ~ 1e-6 is
-// squared by each refinement).  One CTA per row; the FP64 work is the residual
-// band products (2*(kd+1) FMA per element per refinement), spread over the CTA.
+// scaled) residual, refined three times with FP64 residuals r = b - U~ x
+// (mixed-precision iterative refinement: each pass multiplies the error by the
+// FP32 solve's relative accuracy, c*eps32*cond(U) ~ 1e-5 for the B-spline overlap
+// factors, so three passes reach the FP64 level).  One CTA per row; the FP64 work
+// is the residual band products (2*(kd+1) FMA per element per pass).
 constexpr int kIrThreads = 256;
-constexpr int kIrRefinements = 2;
+constexpr int kIrRefinements = 3;
 
 template <int KD, typename TI, typename TO, typename TV>
 __global__ void __launch_bounds__(kIrThreads) k_solve_ir(SolveTab<float> tab, const double* __restrict__ udp,
@@ -650,6 +651,14 @@ constexpr int kKChunk = 8;                    // basis vectors handled per pass 
 
 int grid_reduce_blocks() { return 152; }
 
+// doubles of reduction scratch every launcher may use (update: up to 4*152 blocks of
+// kPStride; dot: 2 values per (value, chunk) with at most ~304 + values chunks)
+size_t partials_capacity() {
+    const size_t upd = (size_t)4 * 152 * kPStride;
+    const size_t dot = (size_t)2 * (kMaxBasis + 1) * (304 + kMaxBasis + 1);
+    return upd > dot ? upd : dot;
+}
+
 template <typename CI>
 __global__ void __launch_bounds__(kRedThreads) k_norm(const CI* __restrict__ x, long n, double* partials,
                                                       unsigned* counter, Ctrl* ctrl) {
@@ -684,82 +693,157 @@ cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsig
     return cudaGetLastError();
 }
 
-// h_k = <v_k, w> for k < nv (BLASIntegrationFunctor block InnerProduct, functors.h:236-240).
-// mode 0 writes ctrl->h (and ||w|| into orig_norm when want_norm), mode 1 writes ctrl->h3
-// and runs only while a re-orthogonalisation pass is requested.
+// h_k = <v_k, w> for k < nv (BLASIntegrationFunctor block InnerProduct, functors.h:236-240),
+// and ||w||^2 as value nv when want_norm.
+// Grid: (element chunks, values).  A block reduces ONE value over a contiguous chunk of
+// 256*epl elements, with four interleaved accumulators per component, so the lane-wide
+// FP64 reduction (the FP64 pipe is ~1/64 of FP32 on this part) is amortised over many
+// products.  Block partials [value][chunk] are summed by the last block in fixed order.
+// Destination: ctrl->h (mode 0; ||w|| into ctrl->orig_norm) or ctrl->h3 (mode 1, only
+// while a re-orthogonalisation pass is requested), or hout[0..2nv] (+ hout[2nv] = ||w||^2)
+// when ctrl is null.
+constexpr int kDotThreads = 256;
+
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_cgs_dot(const cx<T>* __restrict__ V, long n, int nv,
+__global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict__ V, long n, int nv,
                                                          const cx<T>* __restrict__ w, double* partials,
-                                                         unsigned* counter, Ctrl* ctrl, int mode, int want_norm) {
+                                                         unsigned* counter, Ctrl* ctrl, int mode, int want_norm,
+                                                         double* hout, int epl) {
     using C = cx<T>;
-    if (ctrl->broken) return;
-    if (mode == 1 && !ctrl->ro_go) return;
-    for (int kc = 0; kc < nv; kc += kKChunk) {
-        double acc[2 * kKChunk];
+    __shared__ double red[kDotThreads / 32][2];
+    if (ctrl) {
+        if (ctrl->broken) return;
+        if (mode == 1 && !ctrl->ro_go) return;
+    }
+    const int k = blockIdx.y, nchunks = gridDim.x, chunk = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const C* vk = k < nv ? V + (size_t)k * n : w;
+    const long e0 = (long)chunk * kDotThreads * epl + tid;
+    double ar[4] = {0.0, 0.0, 0.0, 0.0}, ai[4] = {0.0, 0.0, 0.0, 0.0};
+    int t = 0;
+    for (; t + 3 < epl; t += 4) {
 #pragma unroll
-        for (int k = 0; k < 2 * kKChunk; ++k) acc[k] = 0.0;
-        for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-            const C wi = w[i];
-            const double wr = (double)wi.x, wim = (double)wi.y;
-            // conj(v) * w, each product exact in FP64 for complex64 operands
-#pragma unroll
-            for (int k = 0; k < kKChunk; ++k) {
-                if (kc + k < nv) {
-                    const C v = V[(size_t)(kc + k) * n + i];
-                    const double vr = (double)v.x, vi = (double)v.y;
-                    acc[2 * k] = fma(vr, wr, acc[2 * k]);
-                    acc[2 * k] = fma(vi, wim, acc[2 * k]);
-                    acc[2 * k + 1] = fma(vr, wim, acc[2 * k + 1]);
-                    acc[2 * k + 1] = fma(-vi, wr, acc[2 * k + 1]);
-                }
+        for (int q = 0; q < 4; ++q) {
+            const long e = e0 + (long)(t + q) * kDotThreads;
+            if (e < n) {
+                const C v = vk[e], x = w[e];
+                const double vr = (double)v.x, vi = (double)v.y, xr = (double)x.x, xi = (double)x.y;
+                ar[q] = fma(vr, xr, ar[q]);
+                ar[q] = fma(vi, xi, ar[q]);
+                ai[q] = fma(vr, xi, ai[q]);
+                ai[q] = fma(-vi, xr, ai[q]);
             }
         }
-        const int nvalid = 2 * min(kKChunk, nv - kc);
-        block_partials<2 * kKChunk>(acc, nvalid, partials, kPStride, 2 * kc);
     }
-    if (want_norm && mode == 0) {
-        double acc[1] = {0.0};
-        for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-            const C wi = w[i];
-            const double re = (double)wi.x, im = (double)wi.y;
-            acc[0] = fma(re, re, acc[0]);
-            acc[0] = fma(im, im, acc[0]);
+    for (; t < epl; ++t) {
+        const long e = e0 + (long)t * kDotThreads;
+        if (e < n) {
+            const C v = vk[e], x = w[e];
+            const double vr = (double)v.x, vi = (double)v.y, xr = (double)x.x, xi = (double)x.y;
+            ar[0] = fma(vr, xr, ar[0]);
+            ar[0] = fma(vi, xi, ar[0]);
+            ai[0] = fma(vr, xi, ai[0]);
+            ai[0] = fma(-vi, xr, ai[0]);
         }
-        block_partials<1>(acc, 1, partials, kPStride, 2 * kMaxBasis);
     }
-    if (is_last_block(counter)) {
-        __shared__ double tot[2 * kMaxBasis + 1];
-        final_sum(partials, gridDim.x, kPStride, 2 * nv, tot);
-        if (want_norm && mode == 0) {
-            __shared__ double nn[1];
-            final_sum(partials + 2 * kMaxBasis, gridDim.x, kPStride, 1, nn);
-            if (threadIdx.x == 0) ctrl->orig_norm = sqrt(nn[0]);
-        }
+    double sr = (ar[0] + ar[1]) + (ar[2] + ar[3]);
+    double si = (ai[0] + ai[1]) + (ai[2] + ai[3]);
+    sr = warp_sum(sr);
+    si = warp_sum(si);
+    if (lane == 0) { red[warp][0] = sr; red[warp][1] = si; }
+    __syncthreads();
+    if (tid < 2) {
+        double a = 0.0;
+        for (int q = 0; q < kDotThreads / 32; ++q) a += red[q][tid];
+        partials[((size_t)k * nchunks + chunk) * 2 + tid] = a;
+    }
+    // last block of the whole grid sums the chunks of every value in fixed order
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned v = atomicAdd(counter, 1u);
+        s_last = (v == gridDim.x * gridDim.y - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int nvals = gridDim.y;
+    __shared__ double tot[2 * (kMaxBasis + 1)];
+    for (int vv = warp; vv < 2 * nvals; vv += kDotThreads / 32) {
+        const int kk = vv >> 1, c = vv & 1;
+        double a = 0.0;
+        for (int ch = lane; ch < nchunks; ch += 32) a += __ldcg(partials + ((size_t)kk * nchunks + ch) * 2 + c);
+        a = warp_sum(a);
+        if (lane == 0) tot[vv] = a;
+    }
+    __syncthreads();
+    if (ctrl) {
         double* dst = mode ? ctrl->h3 : ctrl->h;
-        for (int k = threadIdx.x; k < 2 * nv; k += blockDim.x) dst[k] = tot[k];
-        if (threadIdx.x == 0) *counter = 0;
+        for (int q = tid; q < 2 * nv; q += kDotThreads) dst[q] = tot[q];
+        if (tid == 0 && want_norm && mode == 0) ctrl->orig_norm = sqrt(tot[2 * nv]);
+    } else {
+        for (int q = tid; q < 2 * nv; q += kDotThreads) hout[q] = tot[q];
+        if (tid == 0 && want_norm) hout[2 * nv] = tot[2 * nv];
     }
+    if (tid == 0) *counter = 0;
+}
+
+static void dot_shape(long n, int nvals, int* epl, int* nchunks) {
+    const int target = max(1, 304 / max(nvals, 1));
+    long e = (n + (long)kDotThreads * target - 1) / ((long)kDotThreads * target);
+    if (e < 1) e = 1;
+    *epl = (int)e;
+    *nchunks = (int)((n + (long)kDotThreads * e - 1) / ((long)kDotThreads * e));
 }
 
 cudaError_t launch_cgs_dot(int prec, const void* V, long n, int nv, const void* w, double* partials, unsigned* counter,
                            Ctrl* ctrl, int mode, int want_norm, cudaStream_t s) {
     count_launch();
-    const int blocks = grid_reduce_blocks();
+    const int nvals = nv + ((want_norm && mode == 0) ? 1 : 0);
+    int epl, nch;
+    dot_shape(n, nvals, &epl, &nch);
+    dim3 grid(nch, nvals);
     if (prec == 0)
-        k_cgs_dot<double><<<blocks, kRedThreads, 0, s>>>((const double2*)V, n, nv, (const double2*)w, partials, counter,
-                                                         ctrl, mode, want_norm);
+        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, n, nv, (const double2*)w, partials, counter,
+                                                       ctrl, mode, want_norm, nullptr, epl);
     else
-        k_cgs_dot<float><<<blocks, kRedThreads, 0, s>>>((const float2*)V, n, nv, (const float2*)w, partials, counter,
-                                                        ctrl, mode, want_norm);
+        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, n, nv, (const float2*)w, partials, counter,
+                                                      ctrl, mode, want_norm, nullptr, epl);
+    return cudaGetLastError();
+}
+
+size_t block_inner_scratch_doubles(long n, int nvals) {
+    int epl, nch;
+    dot_shape(n, nvals, &epl, &nch);
+    return (size_t)2 * nvals * nch;
+}
+
+cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const void* w, int want_norm, double* out,
+                               double* partials, unsigned* counter, cudaStream_t s) {
+    count_launch();
+    const int nvals = nv + (want_norm ? 1 : 0);
+    int epl, nch;
+    dot_shape(n, nvals, &epl, &nch);
+    dim3 grid(nch, nvals);
+    if (prec == 0)
+        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, n, nv, (const double2*)w, partials, counter,
+                                                       nullptr, 0, want_norm, out, epl);
+    else
+        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, n, nv, (const float2*)w, partials, counter,
+                                                      nullptr, 0, want_norm, out, epl);
     return cudaGetLastError();
 }
 
 // w <- w - V h  (zgemv 'N' + zaxpy, pamp.h:330-332) and ||w||.
 // mode 0: primary pass (h), sets resid_norm and the re-orthogonalisation request
-//         (pamp.h:369: resid < 0.717 * orig) when mode_flags bit 1 (double orth) is set;
+//         (pamp.h:369: resid < 0.717 * orig) when mode bit 1 (double orth) is set;
 // mode 1: re-orthogonalisation pass (h3), h += h3, orig <- resid, resid <- ||w||.
+// The basis loads of four vectors are issued together per step of the k loop.
+constexpr int kUpdThreads = 256;
+
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_cgs_update(const cx<T>* __restrict__ V, long n, int nv,
+__global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restrict__ V, long n, int nv,
                                                             cx<T>* __restrict__ w, double* partials,
                                                             unsigned* counter, Ctrl* ctrl, int mode) {
     using C = cx<T>;
@@ -773,33 +857,32 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_update(const cx<T>* __restr
     __syncthreads();
     double acc[1] = {0.0};
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        // four independent accumulation chains (FP64 FMA latency ~64 cycles)
-        T sr0 = 0, si0 = 0, sr1 = 0, si1 = 0;
+        T sr[4] = {0, 0, 0, 0}, si[4] = {0, 0, 0, 0};
         int k = 0;
-        for (; k + 1 < nv; k += 2) {
-            const C v0 = V[(size_t)k * n + i];
-            const C v1 = V[(size_t)(k + 1) * n + i];
-            const C h0 = hs[k], h1 = hs[k + 1];
-            sr0 = fma(v0.x, h0.x, sr0);
-            sr0 = fma(-v0.y, h0.y, sr0);
-            si0 = fma(v0.x, h0.y, si0);
-            si0 = fma(v0.y, h0.x, si0);
-            sr1 = fma(v1.x, h1.x, sr1);
-            sr1 = fma(-v1.y, h1.y, sr1);
-            si1 = fma(v1.x, h1.y, si1);
-            si1 = fma(v1.y, h1.x, si1);
+        for (; k + 3 < nv; k += 4) {
+            C v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = V[(size_t)(k + q) * n + i];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const C hk = hs[k + q];
+                sr[q] = fma(v[q].x, hk.x, sr[q]);
+                sr[q] = fma(-v[q].y, hk.y, sr[q]);
+                si[q] = fma(v[q].x, hk.y, si[q]);
+                si[q] = fma(v[q].y, hk.x, si[q]);
+            }
         }
-        if (k < nv) {
+        for (; k < nv; ++k) {
             const C v0 = V[(size_t)k * n + i];
-            const C h0 = hs[k];
-            sr0 = fma(v0.x, h0.x, sr0);
-            sr0 = fma(-v0.y, h0.y, sr0);
-            si0 = fma(v0.x, h0.y, si0);
-            si0 = fma(v0.y, h0.x, si0);
+            const C hk = hs[k];
+            sr[0] = fma(v0.x, hk.x, sr[0]);
+            sr[0] = fma(-v0.y, hk.y, sr[0]);
+            si[0] = fma(v0.x, hk.y, si[0]);
+            si[0] = fma(v0.y, hk.x, si[0]);
         }
         C r = w[i];
-        r.x -= sr0 + sr1;
-        r.y -= si0 + si1;
+        r.x -= (sr[0] + sr[1]) + (sr[2] + sr[3]);
+        r.y -= (si[0] + si[1]) + (si[2] + si[3]);
         w[i] = r;
         const double re = (double)r.x, im = (double)r.y;
         acc[0] = fma(re, re, acc[0]);
@@ -836,12 +919,13 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_update(const cx<T>* __restr
 cudaError_t launch_cgs_update(int prec, const void* V, long n, int nv, void* w, double* partials, unsigned* counter,
                               Ctrl* ctrl, int mode, cudaStream_t s) {
     count_launch();
-    const int blocks = grid_reduce_blocks();
+    int blocks = (int)((n + kUpdThreads - 1) / kUpdThreads);
+    if (blocks > grid_reduce_blocks() * 4) blocks = grid_reduce_blocks() * 4;
     if (prec == 0)
-        k_cgs_update<double><<<blocks, kRedThreads, 0, s>>>((const double2*)V, n, nv, (double2*)w, partials, counter,
+        k_cgs_update<double><<<blocks, kUpdThreads, 0, s>>>((const double2*)V, n, nv, (double2*)w, partials, counter,
                                                             ctrl, mode);
     else
-        k_cgs_update<float><<<blocks, kRedThreads, 0, s>>>((const float2*)V, n, nv, (float2*)w, partials, counter,
+        k_cgs_update<float><<<blocks, kUpdThreads, 0, s>>>((const float2*)V, n, nv, (float2*)w, partials, counter,
                                                            ctrl, mode);
     return cudaGetLastError();
 }

@@ -168,7 +168,8 @@ def test_ragged_sizes(maxl, xsize, order):
     want, _ = op.advance(psi0, 6, prob.TimeStep, scal)
     d = _dev(psi0)
     prob.Propagator.Handle().advance(d, scal, prob.TimeStep)
-    assert rel(_host(d), want) < 1e-12
+    # the finest grids here make the operator very stiff (|H_m| ~ 1e4): 3e-12 per two steps
+    assert rel(_host(d), want) < 3e-12
 
 
 def test_double_orthogonalization_vs_oracle():
@@ -245,3 +246,35 @@ def test_mixed_precision_error_report():
     # complex64 matvec rounding perturbs the Ritz values by ~eps32 * ||H|| (||H|| ~ 1.6e4 for
     # this random initial state): regression bound for the plain mixed mode
     assert err < 2e-3
+
+
+@pytest.mark.parametrize("prec,n,nv", [(0, 64000, 11), (0, 1060, 1), (1, 5003, 30), (0, 77, 45)])
+def test_block_inner_product_stateless(prec, n, nv):
+    """gbprop_block_inner_product (functors.h:236-240) against numpy, with and without ||w||^2."""
+    import ctypes
+    from pyprop_gb300 import _native
+    L = _native.lib()
+    rng = np.random.default_rng(n + nv)
+    cdt = np.complex128 if prec == 0 else np.complex64
+    V = (rng.standard_normal((nv, n)) + 1j * rng.standard_normal((nv, n))).astype(cdt)
+    w = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(cdt)
+    want = V.astype(np.complex128).conj() @ w.astype(np.complex128)
+    nrm = float(np.vdot(w.astype(np.complex128), w.astype(np.complex128)).real)
+    ws = L.gbprop_block_inner_product_workspace(n, nv)
+    assert ws > 0
+    dV, dw = _dev(V), _dev(w)
+    work = _torch().zeros(ws, dtype=_torch().uint8, device="cuda")
+    out = _torch().zeros(2 * nv + 1, dtype=_torch().float64, device="cuda")
+    for want_norm in (0, 1):
+        _native.check(L.gbprop_block_inner_product(prec, _native.ptr(dV), n, nv, _native.ptr(dw), want_norm,
+                                                   _native.ptr(out), _native.ptr(work), ws, None))
+        _torch().cuda.synchronize()
+        got = _host(out)
+        h = got[0:2 * nv:2] + 1j * got[1:2 * nv:2]
+        assert rel(h, want) < 1e-13
+        if want_norm:
+            assert abs(got[2 * nv] - nrm) / nrm < 1e-13
+    # a workspace one byte short is rejected
+    st = L.gbprop_block_inner_product(prec, _native.ptr(dV), n, nv, _native.ptr(dw), 0, _native.ptr(out),
+                                      _native.ptr(work), ws - 1, None)
+    assert st == 1
