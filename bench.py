@@ -34,7 +34,7 @@ CONFIGS = {
 METRIC = "Krylov steps/s (pAMP x TensorPotential step, 1 GB300)"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
-# FP64 FMA issue rate measured on this machine's GB300 (profiles/fp64_fp32_issue_rates.md)
+# FP64 FMA issue rate measured on GB300 with a dependent-free FMA loop over all SMs
 FP64_PEAK_TFLOPS = 1.195
 
 
@@ -327,7 +327,7 @@ def main():
     band_flops = nterms * nr * (2 * prob.psi.GetRepresentation().radial.kd + 1) * 4
     compute = {"unit": "TFLOP/s", "achieved": band_flops / (t_band * 1e-3) / 1e12,
                "peak": FP64_PEAK_TFLOPS if args.precision == "fp64" else 69.9,
-               "peak_source": "measured FMA issue rate (profiles/fp64_fp32_issue_rates.md)"}
+               "peak_source": "measured FMA issue rate on GB300"}
     compute["frac"] = compute["achieved"] / compute["peak"]
     roofline = {
         "bound": "hbm", "kernel": "k_band_apply (TensorPotentialMultiply, all terms)",
