@@ -159,6 +159,23 @@ size_t gbprop_block_inner_product_workspace(long n, int nv);
 gbprop_status gbprop_block_inner_product(int precision, const void* V, long n, int nv, const void* w, int want_norm,
                                          double* out, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Allocation-free variant of gbprop_block_inner_product, for callers that cannot
+ * allocate device memory when they need it: code running while a CUDA graph is
+ * captured (cudaMalloc cannot be captured), memory pools or custom allocators that
+ * call back into this library, hosts that hand over only fixed buffers.  No
+ * counterpart in the reference (its temp vector is always caller-allocated).
+ * Same arguments and results as gbprop_block_inner_product minus the workspace:
+ * the reduction scratch is one fixed array of 1024 doubles + a counter word in
+ * the library's device memory (on every GPU that loads the library, held until
+ * exit).  Calls no cudaMalloc/cudaFree.  Limits: 1 <= nv <= 45, any n > 0; larger
+ * requests are rejected with GBPROP_EINVAL.  The first call on each device looks
+ * up the array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  Every call shares the one
+ * array: calls that overlap on the GPU (different streams, or different host
+ * threads on one device) race and must be serialised by the caller. */
+gbprop_status gbprop_block_inner_product_noalloc(int precision, const void* V, long n, int nv, const void* w,
+                                                 int want_norm, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

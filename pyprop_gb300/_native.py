@@ -68,6 +68,8 @@ _PROTOS = {
     "gbprop_block_inner_product_workspace": (C.c_size_t, [C.c_long, C.c_int]),
     "gbprop_block_inner_product": (C.c_int, [C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
+    "gbprop_block_inner_product_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p, C.c_int,
+                                                     C.c_void_p, C.c_void_p]),
 }
 
 

@@ -36,6 +36,14 @@ gbprop_status fail(gbprop_status st, const std::string& msg) {
     return st;
 }
 
+}  // namespace
+
+namespace gbprop {
+void set_last_error(const char* msg) { t_err = msg ? msg : ""; }
+}  // namespace gbprop
+
+namespace {
+
 #define GB_CUDA(call)                                                                                  \
     do {                                                                                               \
         cudaError_t _e = (call);                                                                       \

@@ -80,6 +80,9 @@ struct SchedEntry {
     double dt_im;
 };
 
+// Message returned by gbprop_last_error() on the calling thread.
+void set_last_error(const char* msg);
+
 // Launch counter shared by all launchers (process-wide).
 void count_launch(int n = 1);
 long long launch_count();
