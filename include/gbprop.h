@@ -137,6 +137,26 @@ gbprop_status gbprop_reset_stats(gbprop_handle h);
 gbprop_status gbprop_get_hessenberg(gbprop_handle h, double* out);
 gbprop_status gbprop_synchronize(gbprop_handle h);
 
+/* Band-kernel tile autotuner: times every tile shape of the TensorPotential matvec
+ * kernel on this handle's operator and keeps the fastest; *variant (if not NULL)
+ * receives its index.  Synchronises the handle's stream. */
+gbprop_status gbprop_autotune(gbprop_handle h, int* variant);
+
+/* Batches of independent problems (each a finalized handle, all of one precision,
+ * each with its own operator, sizes, Krylov size, time function and time step),
+ * advanced together: one step of the batch is a single CUDA graph launch whose
+ * branches are the problems' step sequences.  The handles must outlive the batch.
+ * autotune != 0 runs gbprop_autotune on every member first. */
+typedef struct gbprop_batch_ctx* gbprop_batch;
+gbprop_status gbprop_batch_create(gbprop_batch* out, const gbprop_handle* problems, int count, int autotune,
+                                  void* stream);
+/* psi[p]: DEVICE wavefunction of problem p; scalings: count x nsteps HOST array
+ * (row p = time-function values of problem p at the start of each step);
+ * dt: count x 2 HOST array (re, im of each problem's time step). */
+gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps, const double* scalings,
+                                   const double* dt);
+gbprop_status gbprop_batch_destroy(gbprop_batch b);
+
 /* Stateless kernel ABI: TensorPotentialMultiply_<S0>_BandNH
  * (generator.py:1373-1426 Fortran entry, :1486-1495 C++ wrapper,
  *  TensorPotential.py:106-112 Python call), complex128 DEVICE buffers:

@@ -65,6 +65,10 @@ _PROTOS = {
     "gbprop_synchronize": (C.c_int, [C.c_void_p]),
     "gbprop_tensor_multiply_bandnh": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double,
                                                 C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "gbprop_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "gbprop_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_void_p]),
+    "gbprop_batch_advance": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.c_void_p]),
+    "gbprop_batch_destroy": (C.c_int, [C.c_void_p]),
     "gbprop_block_inner_product_workspace": (C.c_size_t, [C.c_long, C.c_int]),
     "gbprop_block_inner_product": (C.c_int, [C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
@@ -195,6 +199,40 @@ class Handle:
 
     def synchronize(self):
         check(lib().gbprop_synchronize(self._h))
+
+    def autotune(self):
+        v = C.c_int(-1)
+        check(lib().gbprop_autotune(self._h, C.byref(v)))
+        return v.value
+
+
+class Batch:
+    """Owning wrapper of a gbprop_batch over finalized Handles (kept alive here)."""
+
+    def __init__(self, handles, autotune=True, stream=None):
+        L = lib()
+        self.handles = list(handles)
+        arr = (C.c_void_p * len(self.handles))(*[h.raw.value for h in self.handles])
+        b = C.c_void_p()
+        check(L.gbprop_batch_create(C.byref(b), arr, len(self.handles), int(bool(autotune)), C.c_void_p(stream or 0)))
+        self._b = b
+
+    def __del__(self):
+        try:
+            if getattr(self, "_b", None) and self._b.value:
+                lib().gbprop_batch_destroy(self._b)
+                self._b = C.c_void_p()
+        except Exception:
+            pass
+
+    def advance(self, psis, scalings, dts):
+        """psis: list of device tensors; scalings: (count, nsteps); dts: complex per problem."""
+        import numpy as np
+        P = len(self.handles)
+        s = np.ascontiguousarray(np.asarray(scalings, dtype=np.float64).reshape(P, -1))
+        d = np.ascontiguousarray(np.array([[complex(x).real, complex(x).imag] for x in dts], dtype=np.float64))
+        arr = (C.c_void_p * P)(*[p.data_ptr() for p in psis])
+        check(lib().gbprop_batch_advance(self._b, arr, int(s.shape[1]), ptr(s), ptr(d)))
 
 
 def launch_count():

@@ -163,6 +163,71 @@ class BSplineBasis:
                 out.append(term0 + term1)
         return out
 
+    def local_tables(self):
+        """Values of the `order` B-splines that can be non-zero at each quadrature point:
+        first[g] = index of the first of them; (B, dB, d2B)[g, a] for spline first[g] + a.
+        Same three-point recursions and `> eps` guards as the reference (bspline.cpp:26-164),
+        evaluated only on each point's knot span."""
+        if getattr(self, "_local", None) is not None:
+            return self._local
+        t0 = self.knots
+        k = self.order
+        x = self.grid
+        ng = len(x)
+        mu = np.searchsorted(t0, x, side="right") - 1
+        # pad the knot sequence so that splines that do not exist near the ends (removed by
+        # the continuity conditions) can be evaluated and then discarded; index t[i] -> tp[i + k]
+        tp = np.concatenate([np.full(k, t0[0]), t0, np.full(k, t0[-1])])
+
+        class _T:
+            def __getitem__(self, idx):
+                return tp[np.asarray(idx) + k]
+
+        t = _T()
+        levels = [None, np.ones((ng, 1))]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            for q in range(2, k + 1):
+                prev = levels[q - 1]
+                cur = np.zeros((ng, q))
+                for a in range(q):
+                    i = mu - q + 1 + a
+                    if a >= 1:
+                        b0 = prev[:, a - 1]
+                        d0 = t[i + q - 1] - t[i]
+                        cur[:, a] += np.where(b0 > EPS, (x - t[i]) / d0 * b0, 0.0)
+                    if a <= q - 2:
+                        b1 = prev[:, a]
+                        d1 = t[i + q] - t[i + 1]
+                        cur[:, a] += np.where(b1 > EPS, (t[i + q] - x) / d1 * b1, 0.0)
+                levels.append(cur)
+            B = levels[k]
+            D1 = np.zeros((ng, k))
+            D2 = np.zeros((ng, k))
+            for a in range(k):
+                i = mu - k + 1 + a
+                if a >= 1:
+                    p1 = levels[k - 1][:, a - 1]
+                    D1[:, a] += np.where(p1 > EPS, (k - 1.0) / (t[i + k - 1] - t[i]) * p1, 0.0)
+                if a <= k - 2:
+                    p2 = levels[k - 1][:, a]
+                    D1[:, a] -= np.where(p2 > EPS, (k - 1.0) / (t[i + k] - t[i + 1]) * p2, 0.0)
+                if k > 2:
+                    # B^{k-2}_{i}, _{i+1}, _{i+2} at local offsets a-2, a-1, a of level k-2
+                    def lv(off):
+                        return levels[k - 2][:, off] if 0 <= off <= k - 3 else np.zeros(ng)
+                    q1, q2, q3 = lv(a - 2), lv(a - 1), lv(a)
+                    q1 = np.where(q1 > EPS, q1 * ((k - 2.0) / (t[i + k - 2] - t[i])), q1)
+                    q2 = np.where(q2 > EPS, q2 * ((k - 2.0) / (t[i + k - 1] - t[i + 1])), q2)
+                    q3 = np.where(q3 > EPS, q3 * ((k - 2.0) / (t[i + k] - t[i + 2])), q3)
+                    a_ = (k - 1.0) / (t[i + k - 1] - t[i])
+                    d_ = (k - 1.0) / (t[i + k] - t[i + 1])
+                    D2[:, a] += np.where((q1 > EPS) | (q2 > EPS), a_ * (q1 - q2), 0.0)
+                    D2[:, a] -= np.where((q2 > EPS) | (q3 > EPS), d_ * (q2 - q3), 0.0)
+        first = mu - k + 1
+        # splines beyond the basis (index >= count) are zero by construction of the knot span
+        self._local = (first, np.nan_to_num(B), np.nan_to_num(D1), np.nan_to_num(D2))
+        return self._local
+
     def tables(self):
         """(B, dB, d2B) on the global quadrature grid, each (count, ngrid)
         (CreateBSplineTable / CreateBSplineDerivativeTable, bspline.cpp:169-289),
@@ -256,6 +321,34 @@ class BSplineBasis:
         """Overlap matrix S_ij = <B_i|B_j> (BSpline::SetupOverlap, bspline.cpp:781-785)."""
         return self.band_matrix(np.ones_like(self.grid), 0)
 
+    def band_diagonals(self, f_grid, derivative):
+        """The matrix elements of band_matrix as diagonals: D[k + d, i] = M(i, i + d),
+        d = -k..k (k = order - 1), accumulated from each quadrature point's k
+        non-zero splines; the i > j part follows the reference's swap rule
+        M(j, i) = (-1)^n M(i, j) (bspline.cpp:384-392)."""
+        n = self.count
+        k = self.order
+        f = np.asarray(f_grid)
+        dt = np.result_type(f.dtype, np.float64)
+        D = np.zeros((2 * (k - 1) + 1, n), dtype=dt)
+        first, B, D1, D2 = self.local_tables()
+        right = (B, D1, D2)[derivative]
+        wf = self.grid_weights * f
+        sign = (-1.0) ** derivative
+        for a in range(k):
+            i = first + a
+            ok_i = (i >= 0) & (i < n)
+            for b in range(a, k):
+                d = b - a
+                j = i + d
+                ok = ok_i & (j < n)
+                vals = wf * B[:, a] * right[:, b]
+                acc = np.zeros(n, dtype=dt)
+                np.add.at(acc, i[ok], vals[ok])
+                D[k - 1 + d] += acc
+        for d in range(1, k):
+            D[k - 1 - d, d:] = sign * D[k - 1 + d, : n - d]
+        return D
 
 def bspline_from_section(sec):
     """BSPLINE.ApplyConfigSection (BSpline.py:16-44) from a config section."""
@@ -266,6 +359,34 @@ def bspline_from_section(sec):
                                getattr(sec, "left_point_continuity", None),
                                getattr(sec, "right_point_continuity", None))
     return BSplineBasis(bps, order, cont, getattr(sec, "quad_order_additional", 0))
+
+
+def band_cholesky_upper_diagonals(Sdiag, kd):
+    """Upper Cholesky factor from the diagonals of a symmetric band matrix
+    (Sdiag[kd + d, i] = S(i, i+d)); returns Ud[d, i] = U(i, i+d), d = 0..kd."""
+    n = Sdiag.shape[1]
+    Ud = np.zeros((kd + 1, n))
+    for j in range(n):
+        # column j of U: U(i, j) for i in [j-kd, j]
+        d0 = Sdiag[kd, j]
+        for t in range(1, min(kd, j) + 1):
+            d0 -= Ud[t, j - t] ** 2
+        if not d0 > 0:
+            raise np.linalg.LinAlgError("overlap matrix not positive definite at %d" % j)
+        d0 = math.sqrt(d0)
+        Ud[0, j] = d0
+        for dd in range(1, kd + 1):
+            i = j + dd
+            if i >= n:
+                break
+            sv = Sdiag[kd + dd, j]
+            for t in range(1, kd + 1):
+                r = j - t
+                if r < 0 or i - r > kd:
+                    continue
+                sv -= Ud[t, r] * Ud[i - r, r]
+            Ud[dd, j] = sv / d0
+    return Ud
 
 
 def band_cholesky_upper(S, kd):

@@ -100,6 +100,8 @@ struct gbprop_ctx {
     cudaGraphExec_t graph = nullptr;
     const void* graph_psi = nullptr;
     long long graph_launches = 0;
+    int band_variant = 1;             // tile shape of the band kernel (autotuner)
+    int expm_max_cluster = 16;        // 1 when the handle is advanced inside a batch
 
     ~gbprop_ctx() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -326,6 +328,7 @@ gbprop_status upload_band_op(gbprop_ctx* h, const HostBandOp& ho, BandOp<T>* out
     out->nr = h->nr;
     out->kb = ho.kb;
     out->nterms = (int)ho.src.size();
+    out->variant = h->band_variant;
     out->row_ptr = rp;
     out->t_src = src;
     out->t_slot = slot;
@@ -402,12 +405,27 @@ gbprop_status enqueue_step(gbprop_ctx* h, void* psi) {
         }
         GB_LAUNCH(launch_arnoldi_finalize(h->d_ctrl, h->d_H, m, J, h->double_orth, s));
     }
-    GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, s));
+    GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s));
     GB_LAUNCH(launch_combine(kp, V, N, h->d_ctrl, h->d_x, s));
     // psi <- U^-1 (beta0 V y)  (SolveSqrtOverlap(false))
     GB_LAUNCH(ssolve(h, 0, h->d_x, 0, psi, kp));
     GB_LAUNCH(launch_step_end(h->d_ctrl, s));
     return GBPROP_OK;
+}
+
+void drop_graph(gbprop_ctx* h) {
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+        h->graph_psi = nullptr;
+    }
+}
+
+void set_band_variant(gbprop_ctx* h, int v) {
+    h->band_variant = v;
+    h->t64.op.variant = v;
+    h->t32.op.variant = v;
+    drop_graph(h);
 }
 
 gbprop_status ensure_graph(gbprop_ctx* h, void* psi) {
@@ -722,6 +740,35 @@ gbprop_status gbprop_tensor_multiply_bandnh(int storage, const void* V, int npai
     return GBPROP_OK;
 }
 
+gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    const int kp = h->kprec();
+    cudaStream_t s = h->stream;
+    cudaEvent_t e0, e1;
+    GB_CUDA(cudaEventCreate(&e0));
+    GB_CUDA(cudaEventCreate(&e1));
+    GB_CUDA(cudaMemsetAsync(h->d_s, 0, (size_t)h->N * h->kelem(), s));
+    int best = h->band_variant;
+    float best_ms = 1e30f;
+    for (int v = 0; v < band_variant_count(); ++v) {
+        h->t64.op.variant = v;
+        h->t32.op.variant = v;
+        for (int k = 0; k < 3; ++k) GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, nullptr, h->d_ctrl, 1.0, 0, s));
+        GB_CUDA(cudaEventRecord(e0, s));
+        for (int k = 0; k < 10; ++k) GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, nullptr, h->d_ctrl, 1.0, 0, s));
+        GB_CUDA(cudaEventRecord(e1, s));
+        GB_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) { best_ms = ms; best = v; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    set_band_variant(h, best);
+    if (variant) *variant = best;
+    return GBPROP_OK;
+}
+
 size_t gbprop_block_inner_product_workspace(long n, int nv) {
     if (n <= 0 || nv < 1 || nv > kMaxBasis) return 0;
     // partial sums (the launch shape depends on whether ||w||^2 is requested: size for
@@ -746,6 +793,166 @@ gbprop_status gbprop_block_inner_product(int precision, const void* V, long n, i
     GB_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), s));
     GB_LAUNCH(launch_block_inner(precision == GBPROP_FP64 ? 0 : 1, V, n, nv, w, want_norm ? 1 : 0, out, partials,
                                  counter, s));
+    return GBPROP_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: many independent problems advanced together.  The step sequences
+// of all member handles are captured into one CUDA graph (one branch per
+// problem, forked from and joined into the batch stream), so a whole-batch
+// step is a single graph launch and the GPU overlaps the problems' kernels.
+// ---------------------------------------------------------------------------
+struct gbprop_batch_ctx {
+    std::vector<gbprop_handle> hs;
+    cudaStream_t stream = nullptr, ustream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_in = nullptr, ev_out = nullptr;
+    std::vector<cudaEvent_t> ev_join;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<void*> graph_psi;
+    long long graph_launches = 0;
+    ~gbprop_batch_ctx() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (cudaEvent_t e : ev_join) cudaEventDestroy(e);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_out) cudaEventDestroy(ev_out);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+gbprop_status batch_capture(gbprop_batch b, void* const* psi) {
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    GB_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = launch_count();
+    gbprop_status st = GBPROP_OK;
+    cudaError_t e = cudaEventRecord(b->ev_fork, b->stream);
+    for (size_t p = 0; p < b->hs.size() && st == GBPROP_OK && e == cudaSuccess; ++p) {
+        gbprop_ctx* h = b->hs[p];
+        e = cudaStreamWaitEvent(h->stream, b->ev_fork, 0);
+        if (e != cudaSuccess) break;
+        st = enqueue_step(h, psi[p]);
+        if (st) break;
+        e = cudaEventRecord(b->ev_join[p], h->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_join[p], 0);
+    }
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (st) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(GBPROP_ECUDA, std::string("batch capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    b->graph_launches = launch_count() - before;
+    count_launch((int)-b->graph_launches);
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    b->graph_psi.assign(psi, psi + b->hs.size());
+    return GBPROP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbprop_status gbprop_batch_create(gbprop_batch* out, const gbprop_handle* problems, int count, int autotune,
+                                  void* stream) {
+    if (!out) return fail(GBPROP_EINVAL, "null output pointer");
+    *out = nullptr;
+    if (!problems || count < 1) return fail(GBPROP_EINVAL, "a batch needs at least one problem");
+    for (int p = 0; p < count; ++p) {
+        if (gbprop_status st = check_handle(problems[p], true)) return st;
+        if (problems[p]->prec != problems[0]->prec) return fail(GBPROP_EINVAL, "all problems of a batch share one precision");
+        for (int q = 0; q < p; ++q)
+            if (problems[q] == problems[p]) return fail(GBPROP_EINVAL, "a problem appears twice in the batch");
+    }
+    gbprop_batch b = new gbprop_batch_ctx();
+    b->hs.assign(problems, problems + count);
+    b->ustream = (cudaStream_t)stream;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming);
+    b->ev_join.assign(count, nullptr);
+    for (int p = 0; p < count && e == cudaSuccess; ++p) e = cudaEventCreateWithFlags(&b->ev_join[p], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        delete b;
+        return fail(GBPROP_ECUDA, std::string("batch stream/event creation: ") + cudaGetErrorString(e));
+    }
+    for (gbprop_handle h : b->hs) {
+        h->expm_max_cluster = 1;        // other problems fill the GPU: one CTA per exponential
+        drop_graph(h);
+        if (autotune) {
+            gbprop_status st = gbprop_autotune(h, nullptr);
+            if (st) {
+                delete b;
+                return st;
+            }
+        }
+    }
+    *out = b;
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps, const double* scalings,
+                                   const double* dt) {
+    if (!b) return fail(GBPROP_EINVAL, "null batch");
+    if (!psi || !scalings || !dt) return fail(GBPROP_EINVAL, "null argument");
+    if (nsteps < 0) return fail(GBPROP_EINVAL, "negative step count");
+    if (nsteps == 0) return GBPROP_OK;
+    const size_t P = b->hs.size();
+    for (size_t p = 0; p < P; ++p)
+        if (!psi[p]) return fail(GBPROP_EINVAL, "null wavefunction in batch");
+    GB_CUDA(cudaEventRecord(b->ev_in, b->ustream));
+    GB_CUDA(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
+    int done = 0;
+    while (done < nsteps) {
+        int cap = 1 << 30;
+        for (gbprop_handle h : b->hs) cap = std::min(cap, std::max(h->sched_cap, 1024));
+        const int chunk = std::min(nsteps - done, cap);
+        bool recapture = !b->graph;
+        for (size_t p = 0; p < P; ++p) {
+            gbprop_ctx* h = b->hs[p];
+            const int old_cap = h->sched_cap;
+            if (gbprop_status st = ensure_sched(h, chunk)) return st;
+            if (h->sched_cap != old_cap) recapture = true;
+            std::vector<SchedEntry> sched(chunk);
+            for (int k = 0; k < chunk; ++k)
+                sched[k] = {scalings[p * (size_t)nsteps + done + k], dt[2 * p], dt[2 * p + 1]};
+            GB_CUDA(cudaMemcpyAsync(h->d_sched, sched.data(), chunk * sizeof(SchedEntry), cudaMemcpyHostToDevice,
+                                    b->stream));
+            GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), b->stream));
+        }
+        for (size_t p = 0; p < P && !recapture; ++p)
+            if (b->graph_psi[p] != psi[p]) recapture = true;
+        if (recapture)
+            if (gbprop_status st = batch_capture(b, psi)) return st;
+        for (int k = 0; k < chunk; ++k) {
+            GB_CUDA(cudaGraphLaunch(b->graph, b->stream));
+            count_launch((int)b->graph_launches);
+        }
+        done += chunk;
+    }
+    GB_CUDA(cudaEventRecord(b->ev_out, b->stream));
+    GB_CUDA(cudaStreamWaitEvent(b->ustream, b->ev_out, 0));
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_batch_destroy(gbprop_batch b) {
+    if (!b) return GBPROP_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (gbprop_handle h : b->hs) h->expm_max_cluster = 16;
+    delete b;
     return GBPROP_OK;
 }
 

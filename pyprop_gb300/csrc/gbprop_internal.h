@@ -39,6 +39,7 @@ template <typename T> struct SolveTab {
 // slots are real bands stored diagonal-major: (slot*(2kb+1) + d)*nr + i = A(i, i+d-kb).
 template <typename T> struct BandOp {
     int nl, nr, kb, nterms;
+    int variant;             // tile shape of the band kernel (chosen by the autotuner)
     const int* row_ptr;      // nl + 1
     const int* t_src;        // nterms
     const int* t_slot;       // nterms
@@ -117,7 +118,9 @@ cudaError_t launch_cgs_update(int prec, const void* V, long n, int nv, void* w, 
                               unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
 cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, cudaStream_t s);
 cudaError_t launch_step_begin(Ctrl* ctrl, double* H, int m, cudaStream_t s);
-cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s);
+// max_cluster: 16 lets one problem's exponential spread over a thread-block cluster; 1 keeps it on
+// one CTA (batches, where other problems fill the GPU).
+cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s);
 cudaError_t launch_combine(int prec, const void* V, long n, const Ctrl* ctrl, void* out, cudaStream_t s);
 cudaError_t launch_step_end(Ctrl* ctrl, cudaStream_t s);
 cudaError_t launch_tensor_multiply_ref(int storage, const double2* V, int npairs, const int* pairs, int kb,
@@ -126,6 +129,7 @@ cudaError_t launch_tensor_multiply_ref(int storage, const double2* V, int npairs
 cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s);
 
 int grid_reduce_blocks();
+int band_variant_count();
 size_t partials_capacity();
 
 }  // namespace gbprop

@@ -504,34 +504,37 @@ cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, cons
 // ---------------------------------------------------------------------------
 // tensor-potential matvec over the term list (TensorPotentialMultiply_*_BandNH)
 // ---------------------------------------------------------------------------
-constexpr int kBandThreads = 128;
-constexpr int kBandPer = 2;                          // radial elements per thread (i, i + 128)
-constexpr int kBandTile = kBandThreads * kBandPer;   // radial elements per block
+// Tile shapes of the band kernel the autotuner chooses between:
+// (threads per block, radial elements per thread).
+constexpr int kBandVariants = 4;
+__host__ __device__ constexpr int band_threads(int v) { return v == 0 ? 64 : v == 1 ? 128 : v == 2 ? 128 : 256; }
+__host__ __device__ constexpr int band_per(int v) { return v == 0 ? 2 : v == 1 ? 2 : v == 2 ? 4 : 1; }
 
 // One block: destination row l = blockIdx.y, radial tile blockIdx.x.  For every term
 // of row l the source row's tile (with a kb halo) is staged in shared memory; each
-// thread accumulates two elements with the band sum split into even/odd diagonals
-// (eight independent FMA chains per thread to cover the FP64 latency).
-template <typename T, int KB>
-__global__ void __launch_bounds__(kBandThreads) k_band_apply(BandOp<T> op, const cx<T>* __restrict__ x,
-                                                             cx<T>* __restrict__ y, const SchedEntry* __restrict__ sched,
-                                                             const Ctrl* __restrict__ ctrl, double scal_val,
-                                                             int check_broken) {
+// thread accumulates PER elements with the band sum split into even/odd diagonals
+// (four independent FMA chains per element to cover the FP64 latency).
+template <typename T, int KB, int THREADS, int PER>
+__global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T>* __restrict__ x,
+                                                        cx<T>* __restrict__ y, const SchedEntry* __restrict__ sched,
+                                                        const Ctrl* __restrict__ ctrl, double scal_val,
+                                                        int check_broken) {
     using C = cx<T>;
     constexpr int W = 2 * KB + 1;
-    __shared__ C sx[kBandTile + 2 * KB];
+    constexpr int TILE = THREADS * PER;
+    __shared__ C sx[TILE + 2 * KB];
     if (check_broken && ctrl->broken) return;
-    const int l = blockIdx.y, i0 = blockIdx.x * kBandTile, tid = threadIdx.x;
+    const int l = blockIdx.y, i0 = blockIdx.x * TILE, tid = threadIdx.x;
     const int nr = op.nr;
     const double scal = sched ? sched[ctrl->step].scaling : scal_val;
-    T yr[kBandPer], yi[kBandPer];
+    T yr[PER], yi[PER];
 #pragma unroll
-    for (int e = 0; e < kBandPer; ++e) { yr[e] = 0; yi[e] = 0; }
+    for (int e = 0; e < PER; ++e) { yr[e] = 0; yi[e] = 0; }
     const int t0 = op.row_ptr[l], t1 = op.row_ptr[l + 1];
     for (int t = t0; t < t1; ++t) {
         const size_t sbase = (size_t)op.t_src[t] * nr;
         __syncthreads();
-        for (int j = tid; j < kBandTile + 2 * KB; j += kBandThreads) {
+        for (int j = tid; j < TILE + 2 * KB; j += THREADS) {
             const int g = i0 - KB + j;
             sx[j] = (g >= 0 && g < nr) ? x[sbase + g] : mk<T>(0, 0);
         }
@@ -541,8 +544,8 @@ __global__ void __launch_bounds__(kBandThreads) k_band_apply(BandOp<T> op, const
         if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
         const T Cr = (T)cr, Ci = (T)ci;
 #pragma unroll
-        for (int e = 0; e < kBandPer; ++e) {
-            const int li = tid + e * kBandThreads;
+        for (int e = 0; e < PER; ++e) {
+            const int li = tid + e * THREADS;
             const int i = i0 + li;
             if (i < nr) {
                 T a[W];
@@ -568,17 +571,29 @@ __global__ void __launch_bounds__(kBandThreads) k_band_apply(BandOp<T> op, const
         }
     }
 #pragma unroll
-    for (int e = 0; e < kBandPer; ++e) {
-        const int i = i0 + tid + e * kBandThreads;
+    for (int e = 0; e < PER; ++e) {
+        const int i = i0 + tid + e * THREADS;
         if (i < nr) y[(size_t)l * nr + i] = mk<T>(yr[e], yi[e]);
     }
+}
+
+template <typename T, int KB, int V>
+static void band_apply_v(const BandOp<T>& op, const void* x, void* y, const SchedEntry* sched, const Ctrl* ctrl,
+                         double scaling, int check_broken, cudaStream_t s) {
+    constexpr int TH = band_threads(V), PE = band_per(V);
+    dim3 grid((op.nr + TH * PE - 1) / (TH * PE), op.nl);
+    k_band_apply<T, KB, TH, PE><<<grid, TH, 0, s>>>(op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl, scaling, check_broken);
 }
 
 template <typename T, int KB>
 static void band_apply_kb(const BandOp<T>& op, const void* x, void* y, const SchedEntry* sched, const Ctrl* ctrl,
                           double scaling, int check_broken, cudaStream_t s) {
-    dim3 grid((op.nr + kBandTile - 1) / kBandTile, op.nl);
-    k_band_apply<T, KB><<<grid, kBandThreads, 0, s>>>(op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl, scaling, check_broken);
+    switch (op.variant) {
+        case 0: band_apply_v<T, KB, 0>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
+        case 2: band_apply_v<T, KB, 2>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
+        case 3: band_apply_v<T, KB, 3>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
+        default: band_apply_v<T, KB, 1>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
+    }
 }
 
 template <typename T>
@@ -592,6 +607,8 @@ static cudaError_t band_apply_dispatch(const BandOp<T>& op, const void* x, void*
     }
     return cudaGetLastError();
 }
+
+int band_variant_count() { return kBandVariants; }
 
 cudaError_t launch_band_apply(int arith, const void* opv, const void* x, void* y, const SchedEntry* sched,
                               const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s) {
@@ -1567,10 +1584,10 @@ int expm_cluster_size(int m) {
     return g_expm_cluster[m] == 1 ? 0 : g_expm_cluster[m];
 }
 
-cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s) {
+cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s) {
     count_launch();
-    const int cl = expm_cluster_size(m);
-    if (cl == 16) return launch_expm_cl<16>(ctrl, H, m, sched, s);
+    const int cl = max_cluster >= 8 ? expm_cluster_size(m) : 0;
+    if (cl == 16 && max_cluster >= 16) return launch_expm_cl<16>(ctrl, H, m, sched, s);
     if (cl == 8) return launch_expm_cl<8>(ctrl, H, m, sched, s);
     const size_t smem = (size_t)5 * m * m * sizeof(double2);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -68,6 +68,17 @@ def dense_to_bandnh(M, k):
     return out
 
 
+def diagonals_to_bandnh(D, kb):
+    """Diagonals D[kb + d, i] = M(i, i+d) -> BandNH storage, (i, j) at j*(2kb+1) + kb + i - j."""
+    n = D.shape[1]
+    W = 2 * kb + 1
+    out = np.zeros(n * W, dtype=np.result_type(D.dtype, np.complex128))
+    for d in range(-kb, kb + 1):
+        i = np.arange(max(0, -d), min(n, n - d))
+        out[(i + d) * W + kb - d] = D[kb + d, i]
+    return out
+
+
 def bandnh_to_dense(v, n, k):
     W = 2 * k + 1
     M = np.zeros((n, n), dtype=v.dtype)
@@ -148,8 +159,7 @@ class TensorPotential:
         # radial rank first (ranks are projected last to first)
         radial = np.zeros((len(agrid), rad.count * (2 * k + 1)), dtype=np.complex128)
         for a in range(len(agrid)):
-            M = bs.band_matrix(V[a], diff1)
-            radial[a] = dense_to_bandnh(M, k)
+            radial[a] = diagonals_to_bandnh(bs.band_diagonals(V[a], diff1), k)
         if geom0.storage_id == "Simp":
             data = _sph.project_angular(ang.tools, radial, geom0.GetBasisPairs(), diff0)
         else:
