@@ -221,6 +221,98 @@ def cpu_baseline_sample(workload, budget_s=12.0):
             "sample": "%d Krylov steps of the workload in %.1f s (oracle/oracle.c, OpenMP)" % (n, el)}
 
 
+def run_batch(args, rank, world, local):
+    """256 seeded uneven hydrogen-like problems advanced together (one graph launch per batch step)."""
+    import torch
+    from pyprop_gb300 import _native
+    from pyprop_gb300.batch import BatchPropagator, random_batch
+    device = "cuda:%d" % local
+    torch.cuda.set_device(local)
+    prec = _native.FP64 if args.precision == "fp64" else _native.FP32_MIXED
+    t0 = time.perf_counter()
+    probs = random_batch(args.batch_size, seed=20261204 + rank)
+    bp = BatchPropagator(probs, precision=prec, autotune=True, device=device)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(args.flush_mb * (1 << 20) // 4, dtype=torch.float32, device=device)
+    for _ in range(args.warmup):
+        bp.advance(1)
+    torch.cuda.synchronize()
+    _barrier(world)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = _native.launch_count()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        starts[k].record(stream)
+        bp.advance(1)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    _barrier(world)
+    launches = _native.launch_count() - launches0
+    ms = _max_over_ranks(sum(s_.elapsed_time(e) for s_, e in zip(starts, ends)), world)
+    clk = clocks.stop()
+    P = len(probs)
+    value = world * args.steps / (ms / 1e3)
+    # e2e: every problem's state from pinned host memory, one batch step, back to the host
+    elem = 16 if prec == _native.FP64 else 8
+    hosts = [x.detach().cpu().pin_memory() for x in bp.psi]
+    _barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for h, d in zip(hosts, bp.psi):
+            d.copy_(h, non_blocking=True)
+        bp.advance(1)
+        for h, d in zip(hosts, bp.psi):
+            h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = _max_over_ranks(time.perf_counter() - t0, world)
+    nbytes = sum(x.numel() for x in bp.psi) * elem
+    N_tot = sum(p.N for p in probs)
+    B_step = sum(elem * p.N * (p.m * p.m + 7 * p.m + 3) for p in probs)
+    line = {
+        "metric": METRIC + ", batch", "value": value, "unit": "batch steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128" if prec == _native.FP64 else "c64+f64", "data": "synthetic",
+        "config": {"workload": "hydrogen_velocity_batch", "problems": P, "elements": N_tot,
+                   "precision": args.precision, "l2": "flushed between steps (%d MB write)" % args.flush_mb,
+                   "setup_s": setup_s},
+        "problem_steps_per_s": P * value,
+        "e2e": {"value": world * args.steps / e2e_s, "unit": "batch steps/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "step_bytes": {"algorithmic_per_step": B_step, "achieved_GBps": B_step * value / world / 1e9},
+        "clocks": clk, "gpu_launches": launches,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        orc.set_threads(os.cpu_count() or 1)
+        sample = probs[:4]
+        ops = []
+        for p in sample:
+            pots = [dict(kind=orc.ORC_DIAG_BANDNH, data=p.static, pairs=None, timedep=False),
+                    dict(kind=orc.ORC_SIMP_BANDNH, data=p.dipole, pairs=p.pairs, timedep=True)]
+            ops.append((p, orc.Operator(p.nl, p.nr, p.kd, p.kb, p.cholesky_band().astype(np.complex128), pots)))
+        t0 = time.perf_counter()
+        elems = 0
+        n = 0
+        while time.perf_counter() - t0 < 10.0 and n < 200:
+            p, op = ops[n % len(ops)]
+            op.advance(p.initial_state(), p.m, p.dt, [p.field(0.5)])
+            elems += p.N * (p.m * p.m + 7 * p.m + 3)
+            n += 1
+        el = time.perf_counter() - t0
+        # the CPU rate in batch steps/s: the sample's work per second over the whole batch's work per step
+        batch_work = sum(p.N * (p.m * p.m + 7 * p.m + 3) for p in probs)
+        line["cpu_baseline"] = {"value": elems / el / batch_work, "unit": "batch steps/s",
+                                "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": "%d single-problem Krylov steps of the batch's first 4 problems in %.1f s, "
+                                          "scaled by work (N*(m^2+7m+3))" % (n, el)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -228,7 +320,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbprop", choices=["gbprop", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32-mixed"])
-    ap.add_argument("--workload", default="large", choices=list(CONFIGS))
+    ap.add_argument("--workload", default="large", choices=list(CONFIGS) + ["batch"])
+    ap.add_argument("--batch-size", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--flush-mb", type=int, default=512)
     args = ap.parse_args()
@@ -242,6 +335,9 @@ def main():
         dist.init_process_group("nccl" if args.impl == "gbprop" else "gloo")
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "batch":
+        run_batch(args, rank, world, local)
         return
 
     import torch

@@ -485,6 +485,7 @@ gbprop_status gbprop_create(gbprop_handle* out, int nl, int nr, int precision, i
     if (!out) return fail(GBPROP_EINVAL, "null output pointer");
     *out = nullptr;
     if (nl <= 0 || nr <= 0) return fail(GBPROP_EINVAL, "nl and nr must be positive");
+    if (nr > 4096) return fail(GBPROP_EUNSUPPORTED, "radial size above 4096 (one angular row must fit a CTA's shared memory)");
     if (precision != GBPROP_FP64 && precision != GBPROP_FP32_MIXED) return fail(GBPROP_EINVAL, "unknown precision");
     if (krylov_basis_size < 1 || krylov_basis_size > kMaxBasis)
         return fail(GBPROP_EINVAL, "krylov_basis_size must be in [1, 45]");

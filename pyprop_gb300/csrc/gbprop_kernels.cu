@@ -300,22 +300,23 @@ template <int KD, typename TI, typename TO, typename TV>
 __global__ void __launch_bounds__(kIrThreads) k_solve_ir(SolveTab<float> tab, const double* __restrict__ udp,
                                                          const TI* in, TO* out, TV* __restrict__ vstore,
                                                          const Ctrl* __restrict__ ctrl, int scale_mode,
-                                                         int check_broken) {
+                                                         int check_broken, int stage_tables, int stage_udp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = tab.n, L = tab.L, dir = tab.dir;
     double2* bd = reinterpret_cast<double2*>(smem_raw);
     double2* xd = bd + n;
     double2* rd = xd + n;
-    double* ud_s = reinterpret_cast<double*>(rd + n);                 // (KD+1) x n FP64 diagonals
-    float2* rf = reinterpret_cast<float2*>(ud_s + (size_t)(KD + 1) * n);
-    float* tsm = reinterpret_cast<float*>(rf + (size_t)L * kPitch);  // FP32 solve tables
+    float2* rf = reinterpret_cast<float2*>(rd + n);
+    float* tsm = reinterpret_cast<float*>(rf + (size_t)L * kPitch);  // FP32 solve tables (when staged)
+    const int nud = KD * L * 32, ninv = L * 32, ng = KD * L * 32, nm = max(tab.levels, 1) * 32 * KD * KD;
+    double* ud_smem = reinterpret_cast<double*>(tsm + (stage_tables ? nud + ninv + ng + nm : 0));
+    const double* ud_s = stage_udp ? ud_smem : udp;                    // (KD+1) x n FP64 diagonals
     __shared__ float s_red[kIrThreads / 32];
     if (check_broken && ctrl->broken) return;
     const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // stage the solve tables (shared by every row; L2-resident) in shared memory
     SolveTab<float> st = tab;
-    {
-        const int nud = KD * L * 32, ninv = L * 32, ng = KD * L * 32, nm = max(tab.levels, 1) * 32 * KD * KD;
+    if (stage_tables) {
         float* p_ud = tsm;
         float* p_inv = p_ud + nud;
         float* p_g = p_inv + ninv;
@@ -324,12 +325,13 @@ __global__ void __launch_bounds__(kIrThreads) k_solve_ir(SolveTab<float> tab, co
         for (int k = tid; k < ninv; k += kIrThreads) p_inv[k] = tab.invd[k];
         for (int k = tid; k < ng; k += kIrThreads) p_g[k] = tab.g[k];
         for (int k = tid; k < nm; k += kIrThreads) p_m[k] = tab.mlev[k];
-        for (int k = tid; k < (KD + 1) * n; k += kIrThreads) ud_s[k] = udp[k];
         st.ud = p_ud;
         st.invd = p_inv;
         st.g = p_g;
         st.mlev = p_m;
     }
+    if (stage_udp)
+        for (int k = tid; k < (KD + 1) * n; k += kIrThreads) ud_smem[k] = udp[k];
     const double sc = scale_mode ? ctrl->inv_beta : 1.0;
     const size_t base = (size_t)l * n;
     for (int p = tid; p < n; p += kIrThreads) {
@@ -461,16 +463,24 @@ template <int KD>
 static cudaError_t solve_ir_kd(const SolveTab<float>& tab, const double* udp, int nrows, const void* in, int in_prec,
                                void* out, int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode,
                                int check_broken, cudaStream_t s) {
-    const size_t tabf = (size_t)KD * tab.L * 32 * 2 + (size_t)tab.L * 32 + (size_t)(tab.levels > 0 ? tab.levels : 1) * 32 * KD * KD;
-    const size_t smem = (size_t)3 * tab.n * sizeof(double2) + (size_t)(KD + 1) * tab.n * sizeof(double) +
-                        (size_t)tab.L * kPitch * sizeof(float2) + tabf * sizeof(float);
+    // shared memory: b, x, r rows + FP32 work row are required; the solve tables and the FP64
+    // diagonals are staged only while they fit (otherwise read through L1/L2)
+    const size_t limit = 220 * 1024;
+    const size_t base = (size_t)3 * tab.n * sizeof(double2) + (size_t)tab.L * kPitch * sizeof(float2);
+    const size_t tabb = ((size_t)KD * tab.L * 32 * 2 + (size_t)tab.L * 32 +
+                         (size_t)(tab.levels > 0 ? tab.levels : 1) * 32 * KD * KD) * sizeof(float);
+    const size_t udb = (size_t)(KD + 1) * tab.n * sizeof(double);
+    const int stage_tables = base + tabb <= limit;
+    const int stage_udp = base + (stage_tables ? tabb : 0) + udb <= limit;
+    const size_t smem = base + (stage_tables ? tabb : 0) + (stage_udp ? udb : 0);
+    if (smem > limit) return cudaErrorInvalidValue;
     dim3 grid(nrows), block(kIrThreads);
 #define GB_IR_CASE(TI_, TO_, TV_)                                                                                \
     {                                                                                                            \
         auto kern = k_solve_ir<KD, TI_, TO_, TV_>;                                                               \
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
         kern<<<grid, block, smem, s>>>(tab, udp, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,      \
-                                       check_broken);                                                            \
+                                       check_broken, stage_tables, stage_udp);                                   \
         return cudaGetLastError();                                                                               \
     }
     const int key = in_prec * 4 + out_prec * 2 + v_prec;

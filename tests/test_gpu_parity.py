@@ -157,7 +157,8 @@ def test_small_krylov_sizes(m):
     assert rel(_host(d), want) < 1e-12
 
 
-@pytest.mark.parametrize("maxl,xsize,order", [(0, 12, 7), (1, 9, 3), (5, 41, 5), (4, 100, 9), (3, 250, 7)])
+@pytest.mark.parametrize("maxl,xsize,order", [(0, 12, 7), (1, 9, 3), (5, 41, 5), (4, 100, 9), (3, 250, 7),
+                                              (1, 1497, 7)])
 def test_ragged_sizes(maxl, xsize, order):
     """nl = 1 (no dipole pairs), tiny radial sizes (blocks shorter than the band),
     odd sizes and orders 3..9."""
