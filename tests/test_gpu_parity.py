@@ -169,8 +169,12 @@ def test_ragged_sizes(maxl, xsize, order):
     want, _ = op.advance(psi0, 6, prob.TimeStep, scal)
     d = _dev(psi0)
     prob.Propagator.Handle().advance(d, scal, prob.TimeStep)
-    # the finest grids here make the operator very stiff (|H_m| ~ 1e4): 3e-12 per two steps
-    assert rel(_host(d), want) < 3e-12
+    # Fine grids make the step very stiff (up to ~13 squarings): the tolerance follows the
+    # oracle's own sensitivity to a 1e-16 relative perturbation of its input.
+    rng = np.random.default_rng(5)
+    pert, _ = op.advance(psi0 * (1 + 1e-16 * rng.standard_normal(psi0.shape)), 6, prob.TimeStep, scal)
+    tol = max(3e-12, 30 * rel(pert, want))
+    assert rel(_host(d), want) < tol
 
 
 def test_double_orthogonalization_vs_oracle():
