@@ -250,3 +250,39 @@ class Operator:
             for i in range(max(0, j - kd), j + 1):
                 U[i, j] = self.U[j * (kd + 1) + kd + i - j]
         return np.kron(np.eye(self.nl), U)
+
+
+# gradient cross-check (dense) --------------------------------------------------
+def dense_adjoint_gradient(op, psi0, dt, scalings, states, Sfull=None):
+    """Exact discrete gradient of O = sum_b |phi_b^H S psi_T|^2 with respect to the
+    step scalings s_n, for the dense step map psi_{n+1} = U^-1 expm(-i dt A(s_n)) U psi_n,
+    A(s) = U^-H (H0 + s H1) U^-1 (the map the pAMP step approximates, without Krylov
+    truncation; PamPropagator.py:50-57 with the scaling of TensorPotential.py:98-100).
+
+    The reference has no gradient; this dense restatement (scipy expm / expm_frechet,
+    co-state y_n = expm(-i dt A_n)^H y_{n+1}, dO/ds_n = 2 Re y_{n+1}^H L_n x_n with L_n the
+    Frechet derivative of expm at -i dt A_n in direction -i dt A1) checks the GPU adjoint.
+    Returns (O, dO/ds (nsteps,), psi_T)."""
+    import scipy.linalg as sl
+    U = op.dense_U()
+    Ui = np.linalg.inv(U)
+    H0 = op.dense_potential(0.0)
+    H1 = op.dense_potential(1.0) - H0
+    A0 = Ui.conj().T @ H0 @ Ui
+    A1 = Ui.conj().T @ H1 @ Ui
+    S = U.conj().T @ U if Sfull is None else Sfull
+    dt = complex(dt)
+    xs = [U @ np.ascontiguousarray(psi0, dtype=np.complex128).ravel()]
+    for s in scalings:
+        xs.append(sl.expm(-1j * dt * (A0 + s * A1)) @ xs[-1])
+    psi_T = Ui @ xs[-1]
+    phi = np.asarray(states, dtype=np.complex128)
+    amps = phi.conj() @ (S @ psi_T)
+    O = float(np.sum(np.abs(amps) ** 2))
+    y = U @ (phi.T @ amps)
+    g = np.zeros(len(scalings))
+    for n in reversed(range(len(scalings))):
+        E, L = sl.expm_frechet(-1j * dt * (A0 + scalings[n] * A1), -1j * dt * A1)
+        g[n] = 2.0 * np.vdot(y, L @ xs[n]).real
+        y = E.conj().T @ y
+    return O, g, psi_T.reshape(op.nl, op.nr)
