@@ -1,6 +1,6 @@
 """Builds libgbprop.so in-tree (pyprop_gb300/libgbprop.so) for sm_103a with nvcc.
 
-Two translation units compiled in parallel, then linked; no cmake, no torch
+The translation units are compiled in parallel, then linked; no cmake, no torch
 extension machinery.  Re-running is incremental on source mtimes.
 """
 from __future__ import annotations
@@ -15,8 +15,8 @@ PKG = os.path.dirname(HERE)
 ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbprop.so")
-SOURCES = ["gbprop_kernels.cu", "gbprop_api.cpp", "gbprop_noalloc.cu"]
-HEADERS = ["gbprop_internal.h", os.path.join(ROOT, "include", "gbprop.h")]
+SOURCES = ["gbprop_kernels.cu", "gbprop_solve.cu", "gbprop_api.cpp", "gbprop_noalloc.cu"]
+HEADERS = ["gbprop_internal.h", "gbprop_device.cuh", os.path.join(ROOT, "include", "gbprop.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

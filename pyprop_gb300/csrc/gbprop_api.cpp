@@ -15,6 +15,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -102,6 +103,8 @@ struct gbprop_ctx {
     long long graph_launches = 0;
     int band_variant = 1;             // tile shape of the band kernel (autotuner)
     int expm_max_cluster = 16;        // 1 when the handle is advanced inside a batch
+    bool inv_ok = false;              // solves run through the banded approximate inverse
+    InvTab inv[2] = {};               // [0]: U^-1, [1]: U^-T
 
     ~gbprop_ctx() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -221,6 +224,124 @@ HostSolveTab build_solve_tab(const std::vector<double>& U, int n, int kd, int di
                     Mn[B][(size_t)r * kd + c] = acc;
                 }
         M.swap(Mn);
+    }
+    return t;
+}
+
+// ---- banded approximate inverse of the overlap factor ------------------------
+constexpr int kMaxInvBand = 160;      // widest inverse band considered
+constexpr int kMaxRefine = 4;
+
+struct HostInvTab {
+    bool ok = false;
+    int n = 0, kd = 0, w = 0, npad = 0, refine = 0;
+    double contraction = 0.0;          // simulated error ratio of one refinement pass
+    std::vector<float> m;              // (w+1) x npad
+    std::vector<double> u;             // (kd+1) x n
+};
+
+// U~ = U (dir 0) or U^T in reversed coordinates q = n-1-p (dir 1): upper triangular in q.
+// Column c of U~^-1 by back substitution down to row c - Wmax; entries beyond the band whose
+// tail (relative to the row's total) falls below 2^-26 are dropped.  The number of FP64
+// refinement passes is the smallest that brings a simulated solve (FP32 products of the
+// device kernel, FP64 residuals) of a fixed pseudo-random right-hand side to the FP64 level.
+HostInvTab build_inv_tab(const std::vector<double>& U, int n, int kd, int dir) {
+    HostInvTab t;
+    t.n = n;
+    t.kd = kd;
+    t.npad = (n + 3) & ~3;
+    auto ut = [&](int e, int f) -> double {
+        if (dir == 0) return uval(U, n, kd, e, f);
+        return uval(U, n, kd, n - 1 - f, n - 1 - e);
+    };
+    const int W = std::min(n - 1, kMaxInvBand);
+    std::vector<double> inv((size_t)(W + 1) * n, 0.0);        // inv[j*n + q] = U~^-1(q, q+j)
+    std::vector<double> y(n, 0.0);
+    for (int c = 0; c < n; ++c) {
+        const int lo = std::max(0, c - W);
+        for (int i = c; i >= lo; --i) {
+            double s = (i == c) ? 1.0 : 0.0;
+            for (int d = 1; d <= kd && i + d <= c; ++d) s -= ut(i, i + d) * y[i + d];
+            y[i] = s / ut(i, i);
+            inv[(size_t)(c - i) * n + i] = y[i];
+        }
+    }
+    // band width: largest relative tail over rows
+    std::vector<double> tot(n, 0.0), tail(n, 0.0);
+    for (int j = 0; j <= W; ++j)
+        for (int q = 0; q < n; ++q) tot[q] += std::fabs(inv[(size_t)j * n + q]);
+    int w = W;
+    {
+        std::vector<double> acc(n, 0.0);
+        for (int j = W; j >= 1; --j) {
+            double worst = 0.0;
+            for (int q = 0; q < n; ++q) {
+                acc[q] += std::fabs(inv[(size_t)j * n + q]);
+                if (tot[q] > 0) worst = std::max(worst, acc[q] / tot[q]);
+            }
+            if (worst > std::ldexp(1.0, -26)) break;
+            w = j - 1;
+        }
+    }
+    t.w = w;
+    t.m.assign((size_t)(w + 1) * t.npad, 0.0f);
+    for (int j = 0; j <= w; ++j)
+        for (int q = 0; q + j < n; ++q) t.m[(size_t)j * t.npad + q] = (float)inv[(size_t)j * n + q];
+    t.u.assign((size_t)(kd + 1) * n, 0.0);
+    for (int d = 0; d <= kd; ++d)
+        for (int q = 0; q + d < n; ++q) t.u[(size_t)d * n + q] = ut(q, q + d);
+    // simulate the refined solve on a pseudo-random complex right-hand side
+    std::vector<double> br(n), bi(n), xr(n, 0.0), xi(n, 0.0), er(n), ei(n);
+    uint64_t st = 0x9e3779b97f4a7c15ull;
+    auto rnd = [&]() {
+        st = st * 6364136223846793005ull + 1442695040888963407ull;
+        return (double)(int64_t)(st >> 11) / (double)(1ull << 52) - 1.0;
+    };
+    for (int q = 0; q < n; ++q) { br[q] = rnd(); bi[q] = rnd(); }
+    for (int q = n - 1; q >= 0; --q) {                       // exact (FP64) back substitution
+        double sr = br[q], si = bi[q];
+        for (int d = 1; d <= kd && q + d < n; ++d) { sr -= ut(q, q + d) * er[q + d]; si -= ut(q, q + d) * ei[q + d]; }
+        er[q] = sr / ut(q, q);
+        ei[q] = si / ut(q, q);
+    }
+    double xn = 0.0;
+    for (int q = 0; q < n; ++q) xn += er[q] * er[q] + ei[q] * ei[q];
+    xn = std::sqrt(xn);
+    std::vector<float> rr(n + w + 1, 0.f), ri(n + w + 1, 0.f);
+    double prev = 1.0;
+    t.refine = -1;
+    for (int k = 0; k <= kMaxRefine; ++k) {
+        for (int q = 0; q < n; ++q) {
+            double sr = br[q], si = bi[q];
+            for (int d = 0; d <= kd && q + d < n; ++d) { sr -= ut(q, q + d) * xr[q + d]; si -= ut(q, q + d) * xi[q + d]; }
+            rr[q] = (float)sr;
+            ri[q] = (float)si;
+        }
+        for (int q = 0; q < n; ++q) {
+            float a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
+            for (int j = 0; j <= w; ++j) {
+                const float mv = t.m[(size_t)j * t.npad + q];
+                a[j & 3] = std::fma(mv, rr[q + j], a[j & 3]);
+                b[j & 3] = std::fma(mv, ri[q + j], b[j & 3]);
+            }
+            xr[q] += (double)((a[0] + a[1]) + (a[2] + a[3]));
+            xi[q] += (double)((b[0] + b[1]) + (b[2] + b[3]));
+        }
+        double e = 0.0;
+        for (int q = 0; q < n; ++q) e += (xr[q] - er[q]) * (xr[q] - er[q]) + (xi[q] - ei[q]) * (xi[q] - ei[q]);
+        e = std::sqrt(e) / xn;
+        if (k == 1) t.contraction = e / prev;
+        if (k >= 1 && e <= 1e-15) {                // FP64 level reached
+            t.refine = k;
+            t.ok = true;
+            break;
+        }
+        if (k >= 1 && e >= 0.5 * prev) {           // stagnated: the previous pass was the last useful one
+            t.refine = std::max(1, k - 1);
+            t.ok = prev <= 1e-14;
+            break;
+        }
+        prev = e;
     }
     return t;
 }
@@ -350,10 +471,59 @@ gbprop_status check_handle(gbprop_handle h, bool need_final) {
         if (_e != cudaSuccess) return fail(GBPROP_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
     } while (0)
 
+// Chunking of the inverse solve.  `wide` spreads one problem's rows over the GPU: the
+// chunk count minimises (waves of CTAs) x (FP64 residual elements of one CTA, halo
+// included), the refinement being FP64-issue-bound; otherwise (batches, where other
+// problems fill the GPU) the fewest chunks are used.  The chunk's slice of M is staged
+// in shared memory when one CTA's share stays within 200 KB, else M is read through L2.
+void set_inv_chunks(gbprop_ctx* h, bool wide) {
+    const int n = h->nr, kd = h->kd, sms = grid_reduce_blocks();
+    for (int dir = 0; dir < 2; ++dir) {
+        InvTab& t = h->inv[dir];
+        const int P = t.refine, w = t.w;
+        auto chunk_of = [&](int nch) { return std::max(4, ((n + nch - 1) / nch + 3) & ~3); };
+        auto smem_of = [&](int chunk, int stage) {
+            size_t mx = 0;
+            for (int q0 = 0; q0 < n; q0 += chunk) mx = std::max(mx, inv_smem_bytes(n, q0, chunk, P, w, kd, stage, 1));
+            return mx;
+        };
+        auto cost = [&](int chunk) {
+            const int nch = (n + chunk - 1) / chunk;
+            long work = 0;
+            for (int k = 1; k <= P; ++k) work += std::min(n, chunk + (P - k) * (w + kd) + w);
+            const long waves = ((long)h->nl * nch + sms - 1) / sms;
+            return waves * (work + chunk);
+        };
+        int best = -1, best_stage = 0;
+        long best_cost = 0;
+        for (int stage = 1; stage >= 0 && best < 0; --stage) {
+            for (int nch = 1; nch <= 16; ++nch) {
+                const int chunk = chunk_of(nch);
+                if (nch > 1 && chunk < 32) break;
+                if (smem_of(chunk, stage) > (size_t)200 * 1024) continue;
+                const long c = cost(chunk);
+                if (best < 0 || (wide ? c < best_cost : false)) {
+                    best = chunk;
+                    best_cost = c;
+                    best_stage = stage;
+                }
+                if (!wide && best >= 0) break;
+            }
+        }
+        if (best < 0) { best = chunk_of(1); best_stage = 0; }
+        t.chunk = best;
+        t.nchunks = (n + best - 1) / best;
+        t.stage = best_stage;
+    }
+}
+
 // Triangular solve of the Krylov precision: FP64-accurate (FP32 solve + FP64 refinement)
 // for the FP64 path, plain complex64 for the mixed path's basis.
 cudaError_t ksolve(gbprop_ctx* h, int dir, const void* in, int in_prec, void* out, int out_prec, void* vstore,
                    int v_prec, int scale_mode, int check_broken) {
+    if (h->inv_ok)
+        return launch_solve_inv(h->inv[dir], h->nl, h->prec == GBPROP_FP64 ? 1 : 0, in, in_prec, out, out_prec,
+                                vstore, v_prec, h->d_ctrl, dir, scale_mode, check_broken, h->stream);
     if (h->prec == GBPROP_FP64)
         return launch_solve_ir(&h->t32.tab[dir], h->d_ud_phys, h->nl, in, in_prec, out, out_prec, vstore, v_prec,
                                h->d_ctrl, scale_mode, check_broken, h->stream);
@@ -363,6 +533,9 @@ cudaError_t ksolve(gbprop_ctx* h, int dir, const void* in, int in_prec, void* ou
 
 // FP64-accurate solve of the state transforms (both precisions).
 cudaError_t ssolve(gbprop_ctx* h, int dir, const void* in, int in_prec, void* out, int out_prec) {
+    if (h->inv_ok)
+        return launch_solve_inv(h->inv[dir], h->nl, 1, in, in_prec, out, out_prec, nullptr, 0, h->d_ctrl, dir, 0, 0,
+                                h->stream);
     return launch_solve_ir(&h->t32.tab[dir], h->d_ud_phys, h->nl, in, in_prec, out, out_prec, nullptr, 0, h->d_ctrl, 0,
                            0, h->stream);
 }
@@ -570,6 +743,35 @@ gbprop_status gbprop_finalize(gbprop_handle h) {
     for (int dir = 0; dir < 2; ++dir) {
         HostSolveTab ht = build_solve_tab(h->U, h->nr, h->kd, dir);
         if ((st = upload_solve_tab<float>(h, ht, &h->t32.tab[dir]))) return st;
+    }
+    // banded approximate inverse (both directions); the block solve remains for factors
+    // whose inverse decays too slowly.  GBPROP_SOLVER=block selects the block solve.
+    {
+        const char* env = std::getenv("GBPROP_SOLVER");
+        bool use_inv = !(env && std::strcmp(env, "block") == 0);
+        HostInvTab hi[2];
+        for (int dir = 0; dir < 2 && use_inv; ++dir) {
+            hi[dir] = build_inv_tab(h->U, h->nr, h->kd, dir);
+            if (!hi[dir].ok) use_inv = false;
+        }
+        if (use_inv) {
+            for (int dir = 0; dir < 2; ++dir) {
+                InvTab& t = h->inv[dir];
+                t.n = h->nr;
+                t.kd = h->kd;
+                t.w = hi[dir].w;
+                t.npad = hi[dir].npad;
+                t.refine = std::max(hi[0].refine, hi[1].refine);
+                float* dm;
+                double* du;
+                if ((st = h->upload(&dm, hi[dir].m))) return st;
+                if ((st = h->upload(&du, hi[dir].u))) return st;
+                t.m = dm;
+                t.u = du;
+            }
+            set_inv_chunks(h, true);
+            h->inv_ok = true;
+        }
     }
     HostBandOp ho = build_band_op(h);
     if (h->prec == GBPROP_FP64) {
@@ -892,6 +1094,7 @@ gbprop_status gbprop_batch_create(gbprop_batch* out, const gbprop_handle* proble
     }
     for (gbprop_handle h : b->hs) {
         h->expm_max_cluster = 1;        // other problems fill the GPU: one CTA per exponential
+        if (h->inv_ok) set_inv_chunks(h, false);
         drop_graph(h);
         if (autotune) {
             gbprop_status st = gbprop_autotune(h, nullptr);
@@ -952,7 +1155,10 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
 gbprop_status gbprop_batch_destroy(gbprop_batch b) {
     if (!b) return GBPROP_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    for (gbprop_handle h : b->hs) h->expm_max_cluster = 16;
+    for (gbprop_handle h : b->hs) {
+        h->expm_max_cluster = 16;
+        if (h->inv_ok) set_inv_chunks(h, true);
+    }
     delete b;
     return GBPROP_OK;
 }

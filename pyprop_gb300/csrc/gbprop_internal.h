@@ -34,6 +34,47 @@ template <typename T> struct SolveTab {
     const T* mlev;
 };
 
+// Banded approximate inverse of one direction of the overlap-factor solve, in solve
+// coordinates q (q = p for U x = b, q = n-1-p for U^T x = b), where both directions
+// are upper triangular:  U~(q, q+d), d = 0..kd  and  M(q, q+j) ~ U~^-1(q, q+j), j = 0..w.
+// U^-1 of a B-spline overlap factor decays geometrically away from the diagonal, so
+// w is chosen (on the host) where the dropped part is below 2^-26 of the kept one.
+//   m  (j*npad + q)  FP32, zero where q + j >= n;  npad = n rounded up to 4
+//   u  (d*n + q)     FP64, zero where q + d >= n
+// Each CTA owns `chunk` radial elements (a multiple of 4) of one row and recomputes the
+// halo its refinement passes need; stage = 1 keeps the chunk's slice of m in shared memory.
+struct InvTab {
+    int n, kd, w, npad;
+    int chunk, nchunks;
+    int refine;             // FP64-residual refinement passes of the FP64-accurate solve
+    int stage;
+    const float* m;
+    const double* u;
+};
+
+// Region of the CTA whose chunk starts at q0, for P refinement passes: cl elements written,
+// x kept on [q0, q0 + R0), right-hand side read on [q0, q0 + RB).
+__host__ __device__ inline void inv_region(int n, int q0, int chunk, int P, int w, int kd, int* cl, int* R0, int* RB) {
+    const int left = n - q0;
+    *cl = chunk < left ? chunk : left;
+    const int r0 = *cl + P * (w + kd);
+    *R0 = r0 < left ? r0 : left;
+    const int rb = *R0 + w;
+    *RB = rb < left ? rb : left;
+}
+
+// Shared-memory bytes of that CTA: b | x, r (FP64, refined solve only) | M slice (staged) | r32.
+__host__ __device__ inline size_t inv_smem_bytes(int n, int q0, int chunk, int P, int w, int kd, int stage, int r64) {
+    int cl, R0, RB;
+    inv_region(n, q0, chunk, P, w, kd, &cl, &R0, &RB);
+    const int R0p = (R0 + 3) & ~3;
+    size_t b = (size_t)RB * 16;
+    if (r64) b += (size_t)R0 * 16 + (size_t)RB * 16;
+    if (stage) b += (size_t)(w + 1) * R0p * 4;
+    b += (size_t)(R0 + w) * 8;
+    return b;
+}
+
 // Term list of the tensor-potential matvec, grouped by destination row l:
 //   y[l][i] += coef_t * s_t * sum_d slot[t][d][i] * x[src_t][i + d - kb]
 // slots are real bands stored diagonal-major: (slot*(2kb+1) + d)*nr + i = A(i, i+d-kb).
@@ -102,6 +143,13 @@ cudaError_t launch_solve(int arith, const void* tab, int nrows, const void* in, 
 cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, const void* in, int in_prec, void* out,
                             int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
                             cudaStream_t s);
+// Solve through the banded approximate inverse of the overlap factor (see InvTab):
+// x = M b in FP32, then `refine` passes x += M (b - U~ x) with FP64 residuals when
+// refine64 is set (FP64-accurate result); refine64 = 0 gives the plain FP32 solve of the
+// mixed path's Krylov basis.  Grid: (tab.nchunks, nrows); arguments as launch_solve.
+cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
+                             int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int dir, int scale_mode,
+                             int check_broken, cudaStream_t s);
 cudaError_t launch_band_apply(int arith, const void* op, const void* x, void* y, const SchedEntry* sched,
                               const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s);
 cudaError_t launch_tbmv(int arith, int kd, const void* ud_phys, int nl, int nr, const void* in, int in_prec,

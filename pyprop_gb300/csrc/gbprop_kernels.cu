@@ -2,47 +2,22 @@
 // sm_103a (GB300).  On this part FP64 issue rate is ~1/58 of FP32 and a
 // dependent FP64 FMA costs ~64 cycles, so the kernels are shaped to keep FP64
 // work minimal and never put a long FP64 dependency chain on the critical path:
-//   * the banded triangular solves along r (ztbsv in the reference) are block
-//     back-substitutions of length L with the inter-block coupling resolved by
-//     a warp-shuffle suffix scan (precomputed coupling tables), one warp per
-//     angular row;
+//   * the banded triangular solves along r (ztbsv in the reference) live in
+//     gbprop_solve.cu;
 //   * the tensor-potential matvec applies real band slots to complex vectors
 //     (2 FMA per band entry instead of 4) with the source halo tile in smem;
 //   * Gram-Schmidt reductions are two-level (block partials + last-block
 //     finalize in fixed order: deterministic, no atomics on values).
 #include "gbprop_internal.h"
+#include "gbprop_device.cuh"
 
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 
 namespace gbprop {
-
-// ---------------------------------------------------------------------------
-// small complex helpers
-// ---------------------------------------------------------------------------
-template <typename T> __device__ __forceinline__ cx<T> mk(T re, T im);
-template <> __device__ __forceinline__ double2 mk<double>(double re, double im) { return make_double2(re, im); }
-template <> __device__ __forceinline__ float2 mk<float>(float re, float im) { return make_float2(re, im); }
-
-template <typename C> struct elem_of;
-template <> struct elem_of<double2> { using type = double; };
-template <> struct elem_of<float2> { using type = float; };
-
-template <typename CO, typename CI> __device__ __forceinline__ CO conv(CI v) {
-    using E = typename elem_of<CO>::type;
-    CO o;
-    o.x = (E)v.x;
-    o.y = (E)v.y;
-    return o;
-}
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 // Last-block detection for a two-level reduction: every block writes its
 // partials, fences, and bumps `counter`; the block that sees gridDim-1 does
@@ -164,351 +139,6 @@ __device__ void block_partials<16>(double (&acc)[16], int nvalid, double* partia
         partials[(size_t)blockIdx.x * pstride + off + threadIdx.x] = s0 + s1;
     }
     __syncthreads();
-}
-
-// ---------------------------------------------------------------------------
-// parallel banded triangular solve (ztbsv 'U','N' / 'U','C' along r)
-// ---------------------------------------------------------------------------
-constexpr int kPitch = 33;   // smem pitch of the block-interleaved row buffer
-
-// One warp solves U~ x = b for one row held in smem in block-interleaved e order
-// (element e = B*L + i at buf[i*kPitch + B]); lane B owns block B.
-//   1) local back-substitution of the block with rows pre-scaled by 1/U(e,e);
-//   2) warp-shuffle suffix scan of the kd-vector recurrence t_B = y_B[0:kd] - F_B t_{B+1};
-//   3) correction x_B -= G_B t_{B+1}.
-template <typename T, int KD>
-__device__ __forceinline__ void warp_block_solve(const SolveTab<T>& tab, cx<T>* buf, int lane) {
-    using C = cx<T>;
-    const int n = tab.n, L = tab.L, P = tab.P;
-    const int B = lane;
-    C win[KD];
-#pragma unroll
-    for (int d = 0; d < KD; ++d) win[d] = mk<T>(0, 0);
-    for (int i = L - 1; i >= 0; --i) {
-        const int e = B * L + i;
-        const int idx = i * kPitch + B;
-        const T inv = tab.invd[i * 32 + B];
-        C x = mk<T>(0, 0);
-        if (e < n) {
-            const C b = buf[idx];
-            T sr = b.x * inv, si = b.y * inv;
-#pragma unroll
-            for (int d = KD; d >= 1; --d) {
-                const T u = tab.ud[((d - 1) * L + i) * 32 + B];
-                sr = fma(-u, win[d - 1].x, sr);
-                si = fma(-u, win[d - 1].y, si);
-            }
-            x = mk<T>(sr, si);
-            buf[idx] = x;
-        }
-#pragma unroll
-        for (int d = KD - 1; d >= 1; --d) win[d] = win[d - 1];
-        win[0] = x;
-    }
-    C a[KD];
-#pragma unroll
-    for (int c = 0; c < KD; ++c) a[c] = (B * L + c < n && B < P) ? buf[c * kPitch + B] : mk<T>(0, 0);
-    for (int lev = 0; lev < tab.levels; ++lev) {
-        const int s = 1 << lev;
-        C nb[KD];
-#pragma unroll
-        for (int c = 0; c < KD; ++c) {
-            nb[c].x = __shfl_down_sync(0xffffffffu, a[c].x, s);
-            nb[c].y = __shfl_down_sync(0xffffffffu, a[c].y, s);
-        }
-        if (B + s < P) {
-            const T* M = tab.mlev + ((size_t)(lev * 32 + B) * KD) * KD;
-#pragma unroll
-            for (int r = 0; r < KD; ++r) {
-                T ar = a[r].x, ai = a[r].y;
-#pragma unroll
-                for (int c = 0; c < KD; ++c) {
-                    const T mv = M[r * KD + c];
-                    ar = fma(mv, nb[c].x, ar);
-                    ai = fma(mv, nb[c].y, ai);
-                }
-                a[r] = mk<T>(ar, ai);
-            }
-        }
-    }
-    C t[KD];
-#pragma unroll
-    for (int c = 0; c < KD; ++c) {
-        t[c].x = __shfl_down_sync(0xffffffffu, a[c].x, 1);
-        t[c].y = __shfl_down_sync(0xffffffffu, a[c].y, 1);
-    }
-    if (B + 1 < P) {
-        for (int i = 0; i < L; ++i) {
-            const int e = B * L + i;
-            if (e >= n) break;
-            const int idx = i * kPitch + B;
-            C x = buf[idx];
-#pragma unroll
-            for (int c = 0; c < KD; ++c) {
-                const T gv = tab.g[(c * L + i) * 32 + B];
-                x.x = fma(-gv, t[c].x, x.x);
-                x.y = fma(-gv, t[c].y, x.y);
-            }
-            buf[idx] = x;
-        }
-    }
-    __syncwarp();
-}
-
-// Working-precision solve (the complex64 Krylov basis of the mixed path), one warp per row.
-template <typename T, int KD, typename TI, typename TO, typename TV>
-__global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO* out,
-                                              TV* __restrict__ vstore, const Ctrl* __restrict__ ctrl,
-                                              int scale_mode, int check_broken) {
-    using C = cx<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* buf = reinterpret_cast<C*>(smem_raw);
-    if (check_broken && ctrl->broken) return;
-    const int l = blockIdx.x, lane = threadIdx.x;
-    const int n = tab.n, L = tab.L;
-    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
-    const size_t base = (size_t)l * n;
-    for (int p = lane; p < n; p += 32) {
-        TI v = in[base + p];
-        double re = (double)v.x, im = (double)v.y;
-        if (scale_mode) { re *= sc; im *= sc; }
-        C c = mk<T>((T)re, (T)im);
-        if (vstore) vstore[base + p] = conv<TV>(c);
-        const int e = tab.dir ? (n - 1 - p) : p;
-        const int B = e / L, i = e - B * L;
-        buf[i * kPitch + B] = c;
-    }
-    __syncwarp();
-    warp_block_solve<T, KD>(tab, buf, lane);
-    for (int p = lane; p < n; p += 32) {
-        const int e = tab.dir ? (n - 1 - p) : p;
-        const int Bq = e / L, i = e - Bq * L;
-        out[base + p] = conv<TO>(buf[i * kPitch + Bq]);
-    }
-}
-
-// FP64-accurate solve for the FP64 path: FP32 block solve of the (power-of-two
-// scaled) residual, refined three times with FP64 residuals r = b - U~ x
-// (mixed-precision iterative refinement: each pass multiplies the error by the
-// FP32 solve's relative accuracy, c*eps32*cond(U) ~ 1e-5 for the B-spline overlap
-// factors, so three passes reach the FP64 level).  One CTA per row; the FP64 work
-// is the residual band products (2*(kd+1) FMA per element per pass).
-constexpr int kIrThreads = 256;
-constexpr int kIrRefinements = 3;
-
-template <int KD, typename TI, typename TO, typename TV>
-__global__ void __launch_bounds__(kIrThreads) k_solve_ir(SolveTab<float> tab, const double* __restrict__ udp,
-                                                         const TI* in, TO* out, TV* __restrict__ vstore,
-                                                         const Ctrl* __restrict__ ctrl, int scale_mode,
-                                                         int check_broken, int stage_tables, int stage_udp) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n = tab.n, L = tab.L, dir = tab.dir;
-    double2* bd = reinterpret_cast<double2*>(smem_raw);
-    double2* xd = bd + n;
-    double2* rd = xd + n;
-    float2* rf = reinterpret_cast<float2*>(rd + n);
-    float* tsm = reinterpret_cast<float*>(rf + (size_t)L * kPitch);  // FP32 solve tables (when staged)
-    const int nud = KD * L * 32, ninv = L * 32, ng = KD * L * 32, nm = max(tab.levels, 1) * 32 * KD * KD;
-    double* ud_smem = reinterpret_cast<double*>(tsm + (stage_tables ? nud + ninv + ng + nm : 0));
-    const double* ud_s = stage_udp ? ud_smem : udp;                    // (KD+1) x n FP64 diagonals
-    __shared__ float s_red[kIrThreads / 32];
-    if (check_broken && ctrl->broken) return;
-    const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // stage the solve tables (shared by every row; L2-resident) in shared memory
-    SolveTab<float> st = tab;
-    if (stage_tables) {
-        float* p_ud = tsm;
-        float* p_inv = p_ud + nud;
-        float* p_g = p_inv + ninv;
-        float* p_m = p_g + ng;
-        for (int k = tid; k < nud; k += kIrThreads) p_ud[k] = tab.ud[k];
-        for (int k = tid; k < ninv; k += kIrThreads) p_inv[k] = tab.invd[k];
-        for (int k = tid; k < ng; k += kIrThreads) p_g[k] = tab.g[k];
-        for (int k = tid; k < nm; k += kIrThreads) p_m[k] = tab.mlev[k];
-        st.ud = p_ud;
-        st.invd = p_inv;
-        st.g = p_g;
-        st.mlev = p_m;
-    }
-    if (stage_udp)
-        for (int k = tid; k < (KD + 1) * n; k += kIrThreads) ud_smem[k] = udp[k];
-    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
-    const size_t base = (size_t)l * n;
-    for (int p = tid; p < n; p += kIrThreads) {
-        const TI v = in[base + p];
-        double2 b = make_double2((double)v.x, (double)v.y);
-        if (scale_mode) { b.x *= sc; b.y *= sc; }
-        if (vstore) vstore[base + p] = conv<TV>(b);
-        bd[p] = b;
-        rd[p] = b;
-        xd[p] = make_double2(0.0, 0.0);
-    }
-    __syncthreads();
-    for (int it = 0; it <= kIrRefinements; ++it) {
-        if (it > 0) {
-            // r = b - U~ x in FP64 (physical coordinates)
-            for (int p = tid; p < n; p += kIrThreads) {
-                double rr = bd[p].x, ri = bd[p].y;
-                if (dir == 0) {
-#pragma unroll
-                    for (int d = 0; d <= KD; ++d) {
-                        if (p + d < n) {
-                            const double u = ud_s[(size_t)d * n + p];
-                            rr = fma(-u, xd[p + d].x, rr);
-                            ri = fma(-u, xd[p + d].y, ri);
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int d = 0; d <= KD; ++d) {
-                        if (p - d >= 0) {
-                            const double u = ud_s[(size_t)d * n + p - d];
-                            rr = fma(-u, xd[p - d].x, rr);
-                            ri = fma(-u, xd[p - d].y, ri);
-                        }
-                    }
-                }
-                rd[p] = make_double2(rr, ri);
-            }
-            __syncthreads();
-        }
-        // power-of-two scale so that the FP32 right-hand side is O(1)
-        float mx = 0.f;
-        for (int p = tid; p < n; p += kIrThreads) mx = fmaxf(mx, fmaxf(fabsf((float)rd[p].x), fabsf((float)rd[p].y)));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) s_red[warp] = mx;
-        __syncthreads();
-        mx = 0.f;
-#pragma unroll
-        for (int w = 0; w < kIrThreads / 32; ++w) mx = fmaxf(mx, s_red[w]);
-        if (mx == 0.f) break;                       // exact solution reached (or zero rhs)
-        int ex;
-        frexpf(mx, &ex);
-        const double scale = ldexp(1.0, -ex), unscale = ldexp(1.0, ex);
-        for (int p = tid; p < n; p += kIrThreads) {
-            const int e = dir ? (n - 1 - p) : p;
-            const int B = e / L, i = e - B * L;
-            rf[i * kPitch + B] = make_float2((float)(rd[p].x * scale), (float)(rd[p].y * scale));
-        }
-        __syncthreads();
-        if (warp == 0) warp_block_solve<float, KD>(st, rf, lane);
-        __syncthreads();
-        for (int p = tid; p < n; p += kIrThreads) {
-            const int e = dir ? (n - 1 - p) : p;
-            const int B = e / L, i = e - B * L;
-            const float2 dlt = rf[i * kPitch + B];
-            xd[p].x += (double)dlt.x * unscale;
-            xd[p].y += (double)dlt.y * unscale;
-        }
-        __syncthreads();
-    }
-    for (int p = tid; p < n; p += kIrThreads) out[base + p] = conv<TO>(xd[p]);
-}
-
-template <typename T, int KD>
-static cudaError_t solve_kd(const SolveTab<T>& tab, int nrows, const void* in, int in_prec, void* out, int out_prec,
-                            void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
-                            cudaStream_t s) {
-    const size_t smem = (size_t)tab.L * kPitch * sizeof(cx<T>);
-    dim3 grid(nrows), block(32);
-    // in/out/vstore precision combinations used by the runtime
-#define GB_SOLVE_CASE(TI_, TO_, TV_)                                                                             \
-    {                                                                                                            \
-        auto kern = k_solve<T, KD, TI_, TO_, TV_>;                                                               \
-        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,           \
-                                       check_broken);                                                            \
-        return cudaGetLastError();                                                                               \
-    }
-    const int key = in_prec * 4 + out_prec * 2 + v_prec;
-    switch (key) {
-        case 0: GB_SOLVE_CASE(double2, double2, double2)
-        case 1: GB_SOLVE_CASE(double2, double2, float2)
-        case 2: GB_SOLVE_CASE(double2, float2, double2)
-        case 3: GB_SOLVE_CASE(double2, float2, float2)
-        case 4: GB_SOLVE_CASE(float2, double2, double2)
-        case 5: GB_SOLVE_CASE(float2, double2, float2)
-        case 6: GB_SOLVE_CASE(float2, float2, double2)
-        default: GB_SOLVE_CASE(float2, float2, float2)
-    }
-#undef GB_SOLVE_CASE
-}
-
-template <typename T>
-static cudaError_t solve_dispatch(const SolveTab<T>& tab, int nrows, const void* in, int in_prec, void* out,
-                                  int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode,
-                                  int check_broken, cudaStream_t s) {
-    switch (tab.kd) {
-#define GB_KD(K) \
-    case K: return solve_kd<T, K>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, scale_mode, check_broken, s);
-        GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
-#undef GB_KD
-        default: return cudaErrorInvalidValue;
-    }
-}
-
-cudaError_t launch_solve(int arith, const void* tab, int nrows, const void* in, int in_prec, void* out, int out_prec,
-                         void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
-                         cudaStream_t s) {
-    count_launch();
-    if (arith == 0)
-        return solve_dispatch(*(const SolveTab<double>*)tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl,
-                              scale_mode, check_broken, s);
-    return solve_dispatch(*(const SolveTab<float>*)tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl,
-                          scale_mode, check_broken, s);
-}
-
-template <int KD>
-static cudaError_t solve_ir_kd(const SolveTab<float>& tab, const double* udp, int nrows, const void* in, int in_prec,
-                               void* out, int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode,
-                               int check_broken, cudaStream_t s) {
-    // shared memory: b, x, r rows + FP32 work row are required; the solve tables and the FP64
-    // diagonals are staged only while they fit (otherwise read through L1/L2)
-    const size_t limit = 220 * 1024;
-    const size_t base = (size_t)3 * tab.n * sizeof(double2) + (size_t)tab.L * kPitch * sizeof(float2);
-    const size_t tabb = ((size_t)KD * tab.L * 32 * 2 + (size_t)tab.L * 32 +
-                         (size_t)(tab.levels > 0 ? tab.levels : 1) * 32 * KD * KD) * sizeof(float);
-    const size_t udb = (size_t)(KD + 1) * tab.n * sizeof(double);
-    const int stage_tables = base + tabb <= limit;
-    const int stage_udp = base + (stage_tables ? tabb : 0) + udb <= limit;
-    const size_t smem = base + (stage_tables ? tabb : 0) + (stage_udp ? udb : 0);
-    if (smem > limit) return cudaErrorInvalidValue;
-    dim3 grid(nrows), block(kIrThreads);
-#define GB_IR_CASE(TI_, TO_, TV_)                                                                                \
-    {                                                                                                            \
-        auto kern = k_solve_ir<KD, TI_, TO_, TV_>;                                                               \
-        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        kern<<<grid, block, smem, s>>>(tab, udp, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,      \
-                                       check_broken, stage_tables, stage_udp);                                   \
-        return cudaGetLastError();                                                                               \
-    }
-    const int key = in_prec * 4 + out_prec * 2 + v_prec;
-    switch (key) {
-        case 0: GB_IR_CASE(double2, double2, double2)
-        case 1: GB_IR_CASE(double2, double2, float2)
-        case 2: GB_IR_CASE(double2, float2, double2)
-        case 3: GB_IR_CASE(double2, float2, float2)
-        case 4: GB_IR_CASE(float2, double2, double2)
-        case 5: GB_IR_CASE(float2, double2, float2)
-        case 6: GB_IR_CASE(float2, float2, double2)
-        default: GB_IR_CASE(float2, float2, float2)
-    }
-#undef GB_IR_CASE
-}
-
-cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, const void* in, int in_prec, void* out,
-                            int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
-                            cudaStream_t s) {
-    count_launch();
-    const SolveTab<float>& tab = *(const SolveTab<float>*)tabf;
-    switch (tab.kd) {
-#define GB_KD(K) \
-    case K: return solve_ir_kd<K>(tab, udp, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, scale_mode, check_broken, s);
-        GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
-#undef GB_KD
-        default: return cudaErrorInvalidValue;
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -674,7 +304,6 @@ cudaError_t launch_tbmv(int arith, int kd, const void* ud, int nl, int nr, const
 // ---------------------------------------------------------------------------
 constexpr int kRedThreads = 512;
 constexpr int kPStride = 2 * kMaxBasis + 4;   // doubles of partials per block
-constexpr int kKChunk = 8;                    // basis vectors handled per pass over w
 
 int grid_reduce_blocks() { return 152; }
 

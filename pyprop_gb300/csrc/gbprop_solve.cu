@@ -1,0 +1,598 @@
+// Banded triangular solves along r (ztbsv 'U','N' / 'U','C' in the reference,
+// piram/piram/blitzblas.h:454-487, called from overlapmatrix.cpp:137-229):
+//   * k_solve_inv   -- banded approximate inverse of the overlap factor applied in FP32
+//                      with FP64-residual refinement (the runtime's default);
+//   * k_solve_ir    -- FP32 block back-substitution + FP64 refinement (fallback for
+//                      factors whose inverse decays too slowly);
+//   * k_solve       -- the block back-substitution in one precision.
+#include "gbprop_internal.h"
+#include "gbprop_device.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace gbprop {
+
+// ---------------------------------------------------------------------------
+// parallel banded triangular solve (ztbsv 'U','N' / 'U','C' along r)
+// ---------------------------------------------------------------------------
+constexpr int kPitch = 33;   // smem pitch of the block-interleaved row buffer
+
+// One warp solves U~ x = b for one row held in smem in block-interleaved e order
+// (element e = B*L + i at buf[i*kPitch + B]); lane B owns block B.
+//   1) local back-substitution of the block with rows pre-scaled by 1/U(e,e);
+//   2) warp-shuffle suffix scan of the kd-vector recurrence t_B = y_B[0:kd] - F_B t_{B+1};
+//   3) correction x_B -= G_B t_{B+1}.
+template <typename T, int KD>
+__device__ __forceinline__ void warp_block_solve(const SolveTab<T>& tab, cx<T>* buf, int lane) {
+    using C = cx<T>;
+    const int n = tab.n, L = tab.L, P = tab.P;
+    const int B = lane;
+    C win[KD];
+#pragma unroll
+    for (int d = 0; d < KD; ++d) win[d] = mk<T>(0, 0);
+    for (int i = L - 1; i >= 0; --i) {
+        const int e = B * L + i;
+        const int idx = i * kPitch + B;
+        const T inv = tab.invd[i * 32 + B];
+        C x = mk<T>(0, 0);
+        if (e < n) {
+            const C b = buf[idx];
+            T sr = b.x * inv, si = b.y * inv;
+#pragma unroll
+            for (int d = KD; d >= 1; --d) {
+                const T u = tab.ud[((d - 1) * L + i) * 32 + B];
+                sr = fma(-u, win[d - 1].x, sr);
+                si = fma(-u, win[d - 1].y, si);
+            }
+            x = mk<T>(sr, si);
+            buf[idx] = x;
+        }
+#pragma unroll
+        for (int d = KD - 1; d >= 1; --d) win[d] = win[d - 1];
+        win[0] = x;
+    }
+    C a[KD];
+#pragma unroll
+    for (int c = 0; c < KD; ++c) a[c] = (B * L + c < n && B < P) ? buf[c * kPitch + B] : mk<T>(0, 0);
+    for (int lev = 0; lev < tab.levels; ++lev) {
+        const int s = 1 << lev;
+        C nb[KD];
+#pragma unroll
+        for (int c = 0; c < KD; ++c) {
+            nb[c].x = __shfl_down_sync(0xffffffffu, a[c].x, s);
+            nb[c].y = __shfl_down_sync(0xffffffffu, a[c].y, s);
+        }
+        if (B + s < P) {
+            const T* M = tab.mlev + ((size_t)(lev * 32 + B) * KD) * KD;
+#pragma unroll
+            for (int r = 0; r < KD; ++r) {
+                T ar = a[r].x, ai = a[r].y;
+#pragma unroll
+                for (int c = 0; c < KD; ++c) {
+                    const T mv = M[r * KD + c];
+                    ar = fma(mv, nb[c].x, ar);
+                    ai = fma(mv, nb[c].y, ai);
+                }
+                a[r] = mk<T>(ar, ai);
+            }
+        }
+    }
+    C t[KD];
+#pragma unroll
+    for (int c = 0; c < KD; ++c) {
+        t[c].x = __shfl_down_sync(0xffffffffu, a[c].x, 1);
+        t[c].y = __shfl_down_sync(0xffffffffu, a[c].y, 1);
+    }
+    if (B + 1 < P) {
+        for (int i = 0; i < L; ++i) {
+            const int e = B * L + i;
+            if (e >= n) break;
+            const int idx = i * kPitch + B;
+            C x = buf[idx];
+#pragma unroll
+            for (int c = 0; c < KD; ++c) {
+                const T gv = tab.g[(c * L + i) * 32 + B];
+                x.x = fma(-gv, t[c].x, x.x);
+                x.y = fma(-gv, t[c].y, x.y);
+            }
+            buf[idx] = x;
+        }
+    }
+    __syncwarp();
+}
+
+// Working-precision solve (the complex64 Krylov basis of the mixed path), one warp per row.
+template <typename T, int KD, typename TI, typename TO, typename TV>
+__global__ void __launch_bounds__(32) k_solve(SolveTab<T> tab, const TI* in, TO* out,
+                                              TV* __restrict__ vstore, const Ctrl* __restrict__ ctrl,
+                                              int scale_mode, int check_broken) {
+    using C = cx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* buf = reinterpret_cast<C*>(smem_raw);
+    if (check_broken && ctrl->broken) return;
+    const int l = blockIdx.x, lane = threadIdx.x;
+    const int n = tab.n, L = tab.L;
+    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
+    const size_t base = (size_t)l * n;
+    for (int p = lane; p < n; p += 32) {
+        TI v = in[base + p];
+        double re = (double)v.x, im = (double)v.y;
+        if (scale_mode) { re *= sc; im *= sc; }
+        C c = mk<T>((T)re, (T)im);
+        if (vstore) vstore[base + p] = conv<TV>(c);
+        const int e = tab.dir ? (n - 1 - p) : p;
+        const int B = e / L, i = e - B * L;
+        buf[i * kPitch + B] = c;
+    }
+    __syncwarp();
+    warp_block_solve<T, KD>(tab, buf, lane);
+    for (int p = lane; p < n; p += 32) {
+        const int e = tab.dir ? (n - 1 - p) : p;
+        const int Bq = e / L, i = e - Bq * L;
+        out[base + p] = conv<TO>(buf[i * kPitch + Bq]);
+    }
+}
+
+// FP64-accurate solve for the FP64 path: FP32 block solve of the (power-of-two
+// scaled) residual, refined three times with FP64 residuals r = b - U~ x
+// (mixed-precision iterative refinement: each pass multiplies the error by the
+// FP32 solve's relative accuracy, c*eps32*cond(U) ~ 1e-5 for the B-spline overlap
+// factors, so three passes reach the FP64 level).  One CTA per row; the FP64 work
+// is the residual band products (2*(kd+1) FMA per element per pass).
+constexpr int kIrThreads = 256;
+constexpr int kIrRefinements = 3;
+
+template <int KD, typename TI, typename TO, typename TV>
+__global__ void __launch_bounds__(kIrThreads) k_solve_ir(SolveTab<float> tab, const double* __restrict__ udp,
+                                                         const TI* in, TO* out, TV* __restrict__ vstore,
+                                                         const Ctrl* __restrict__ ctrl, int scale_mode,
+                                                         int check_broken, int stage_tables, int stage_udp) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = tab.n, L = tab.L, dir = tab.dir;
+    double2* bd = reinterpret_cast<double2*>(smem_raw);
+    double2* xd = bd + n;
+    double2* rd = xd + n;
+    float2* rf = reinterpret_cast<float2*>(rd + n);
+    float* tsm = reinterpret_cast<float*>(rf + (size_t)L * kPitch);  // FP32 solve tables (when staged)
+    const int nud = KD * L * 32, ninv = L * 32, ng = KD * L * 32, nm = max(tab.levels, 1) * 32 * KD * KD;
+    double* ud_smem = reinterpret_cast<double*>(tsm + (stage_tables ? nud + ninv + ng + nm : 0));
+    const double* ud_s = stage_udp ? ud_smem : udp;                    // (KD+1) x n FP64 diagonals
+    __shared__ float s_red[kIrThreads / 32];
+    if (check_broken && ctrl->broken) return;
+    const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // stage the solve tables (shared by every row; L2-resident) in shared memory
+    SolveTab<float> st = tab;
+    if (stage_tables) {
+        float* p_ud = tsm;
+        float* p_inv = p_ud + nud;
+        float* p_g = p_inv + ninv;
+        float* p_m = p_g + ng;
+        for (int k = tid; k < nud; k += kIrThreads) p_ud[k] = tab.ud[k];
+        for (int k = tid; k < ninv; k += kIrThreads) p_inv[k] = tab.invd[k];
+        for (int k = tid; k < ng; k += kIrThreads) p_g[k] = tab.g[k];
+        for (int k = tid; k < nm; k += kIrThreads) p_m[k] = tab.mlev[k];
+        st.ud = p_ud;
+        st.invd = p_inv;
+        st.g = p_g;
+        st.mlev = p_m;
+    }
+    if (stage_udp)
+        for (int k = tid; k < (KD + 1) * n; k += kIrThreads) ud_smem[k] = udp[k];
+    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
+    const size_t base = (size_t)l * n;
+    for (int p = tid; p < n; p += kIrThreads) {
+        const TI v = in[base + p];
+        double2 b = make_double2((double)v.x, (double)v.y);
+        if (scale_mode) { b.x *= sc; b.y *= sc; }
+        if (vstore) vstore[base + p] = conv<TV>(b);
+        bd[p] = b;
+        rd[p] = b;
+        xd[p] = make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    for (int it = 0; it <= kIrRefinements; ++it) {
+        if (it > 0) {
+            // r = b - U~ x in FP64 (physical coordinates)
+            for (int p = tid; p < n; p += kIrThreads) {
+                double rr = bd[p].x, ri = bd[p].y;
+                if (dir == 0) {
+#pragma unroll
+                    for (int d = 0; d <= KD; ++d) {
+                        if (p + d < n) {
+                            const double u = ud_s[(size_t)d * n + p];
+                            rr = fma(-u, xd[p + d].x, rr);
+                            ri = fma(-u, xd[p + d].y, ri);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int d = 0; d <= KD; ++d) {
+                        if (p - d >= 0) {
+                            const double u = ud_s[(size_t)d * n + p - d];
+                            rr = fma(-u, xd[p - d].x, rr);
+                            ri = fma(-u, xd[p - d].y, ri);
+                        }
+                    }
+                }
+                rd[p] = make_double2(rr, ri);
+            }
+            __syncthreads();
+        }
+        // power-of-two scale so that the FP32 right-hand side is O(1)
+        float mx = 0.f;
+        for (int p = tid; p < n; p += kIrThreads) mx = fmaxf(mx, fmaxf(fabsf((float)rd[p].x), fabsf((float)rd[p].y)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) s_red[warp] = mx;
+        __syncthreads();
+        mx = 0.f;
+#pragma unroll
+        for (int w = 0; w < kIrThreads / 32; ++w) mx = fmaxf(mx, s_red[w]);
+        if (mx == 0.f) break;                       // exact solution reached (or zero rhs)
+        int ex;
+        frexpf(mx, &ex);
+        const double scale = ldexp(1.0, -ex), unscale = ldexp(1.0, ex);
+        for (int p = tid; p < n; p += kIrThreads) {
+            const int e = dir ? (n - 1 - p) : p;
+            const int B = e / L, i = e - B * L;
+            rf[i * kPitch + B] = make_float2((float)(rd[p].x * scale), (float)(rd[p].y * scale));
+        }
+        __syncthreads();
+        if (warp == 0) warp_block_solve<float, KD>(st, rf, lane);
+        __syncthreads();
+        for (int p = tid; p < n; p += kIrThreads) {
+            const int e = dir ? (n - 1 - p) : p;
+            const int B = e / L, i = e - B * L;
+            const float2 dlt = rf[i * kPitch + B];
+            xd[p].x += (double)dlt.x * unscale;
+            xd[p].y += (double)dlt.y * unscale;
+        }
+        __syncthreads();
+    }
+    for (int p = tid; p < n; p += kIrThreads) out[base + p] = conv<TO>(xd[p]);
+}
+
+template <typename T, int KD>
+static cudaError_t solve_kd(const SolveTab<T>& tab, int nrows, const void* in, int in_prec, void* out, int out_prec,
+                            void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
+                            cudaStream_t s) {
+    const size_t smem = (size_t)tab.L * kPitch * sizeof(cx<T>);
+    dim3 grid(nrows), block(32);
+    // in/out/vstore precision combinations used by the runtime
+#define GB_SOLVE_CASE(TI_, TO_, TV_)                                                                             \
+    {                                                                                                            \
+        auto kern = k_solve<T, KD, TI_, TO_, TV_>;                                                               \
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,           \
+                                       check_broken);                                                            \
+        return cudaGetLastError();                                                                               \
+    }
+    // combinations the runtime uses (the complex64 Krylov basis of the mixed path)
+    const int key = in_prec * 4 + out_prec * 2 + v_prec;
+    switch (key) {
+        case 3: GB_SOLVE_CASE(double2, float2, float2)
+        case 7: GB_SOLVE_CASE(float2, float2, float2)
+        default: return cudaErrorInvalidValue;
+    }
+#undef GB_SOLVE_CASE
+}
+
+template <typename T>
+static cudaError_t solve_dispatch(const SolveTab<T>& tab, int nrows, const void* in, int in_prec, void* out,
+                                  int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode,
+                                  int check_broken, cudaStream_t s) {
+    switch (tab.kd) {
+#define GB_KD(K) \
+    case K: return solve_kd<T, K>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, scale_mode, check_broken, s);
+        GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
+#undef GB_KD
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_solve(int arith, const void* tab, int nrows, const void* in, int in_prec, void* out, int out_prec,
+                         void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
+                         cudaStream_t s) {
+    count_launch();
+    if (arith == 0) return cudaErrorInvalidValue;     // FP64 solves go through the refined kernels
+    return solve_dispatch(*(const SolveTab<float>*)tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl,
+                          scale_mode, check_broken, s);
+}
+
+template <int KD>
+static cudaError_t solve_ir_kd(const SolveTab<float>& tab, const double* udp, int nrows, const void* in, int in_prec,
+                               void* out, int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode,
+                               int check_broken, cudaStream_t s) {
+    // shared memory: b, x, r rows + FP32 work row are required; the solve tables and the FP64
+    // diagonals are staged only while they fit (otherwise read through L1/L2)
+    const size_t limit = 220 * 1024;
+    const size_t base = (size_t)3 * tab.n * sizeof(double2) + (size_t)tab.L * kPitch * sizeof(float2);
+    const size_t tabb = ((size_t)KD * tab.L * 32 * 2 + (size_t)tab.L * 32 +
+                         (size_t)(tab.levels > 0 ? tab.levels : 1) * 32 * KD * KD) * sizeof(float);
+    const size_t udb = (size_t)(KD + 1) * tab.n * sizeof(double);
+    const int stage_tables = base + tabb <= limit;
+    const int stage_udp = base + (stage_tables ? tabb : 0) + udb <= limit;
+    const size_t smem = base + (stage_tables ? tabb : 0) + (stage_udp ? udb : 0);
+    if (smem > limit) return cudaErrorInvalidValue;
+    dim3 grid(nrows), block(kIrThreads);
+#define GB_IR_CASE(TI_, TO_, TV_)                                                                                \
+    {                                                                                                            \
+        auto kern = k_solve_ir<KD, TI_, TO_, TV_>;                                                               \
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        kern<<<grid, block, smem, s>>>(tab, udp, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,      \
+                                       check_broken, stage_tables, stage_udp);                                   \
+        return cudaGetLastError();                                                                               \
+    }
+    // combinations the runtime uses: refined solves store double2 (or nothing)
+    const int key = in_prec * 4 + out_prec * 2 + v_prec;
+    switch (key) {
+        case 0: GB_IR_CASE(double2, double2, double2)
+        case 2: GB_IR_CASE(double2, float2, double2)
+        case 4: GB_IR_CASE(float2, double2, double2)
+        case 6: GB_IR_CASE(float2, float2, double2)
+        default: return cudaErrorInvalidValue;
+    }
+#undef GB_IR_CASE
+}
+
+cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, const void* in, int in_prec, void* out,
+                            int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int scale_mode, int check_broken,
+                            cudaStream_t s) {
+    count_launch();
+    const SolveTab<float>& tab = *(const SolveTab<float>*)tabf;
+    switch (tab.kd) {
+#define GB_KD(K) \
+    case K: return solve_ir_kd<K>(tab, udp, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, scale_mode, check_broken, s);
+        GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
+#undef GB_KD
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// solve through the banded approximate inverse (all threads busy, no recursion)
+// ---------------------------------------------------------------------------
+// CTA (chunk c, row l) produces x on q in [q0, q0 + cl), q0 = c * chunk.  With P
+// refinement passes, pass k (0..P) updates x on [q0, q0 + R_k), R_k = cl + (P-k)(w+kd):
+//     r = b - U~ x          (FP64; pass 0: r = b, x = 0)
+//     x += 2^e * M (2^-e r) (FP32 products and sums; 2^-e scales max|r| below 1)
+// x on R_k needs r on R_k + w, which needs the previous x on R_k + w + kd = R_{k-1}, so
+// the chunk's halo is recomputed instead of exchanged.  Every element of the region is
+// independent inside a pass: one thread per element, two barriers per pass.
+constexpr int kInvThreads = 256;
+
+template <bool STAGE>
+__device__ __forceinline__ float2 inv_apply(const float* mrow, size_t mstride, const float2* r32, int q, int w) {
+    float ar0 = 0.f, ai0 = 0.f, ar1 = 0.f, ai1 = 0.f, ar2 = 0.f, ai2 = 0.f, ar3 = 0.f, ai3 = 0.f;
+    int j = 0;
+    for (; j + 3 <= w; j += 4) {
+        float m0, m1, m2, m3;
+        if (STAGE) {
+            m0 = mrow[(size_t)j * mstride];
+            m1 = mrow[(size_t)(j + 1) * mstride];
+            m2 = mrow[(size_t)(j + 2) * mstride];
+            m3 = mrow[(size_t)(j + 3) * mstride];
+        } else {
+            m0 = __ldg(mrow + (size_t)j * mstride);
+            m1 = __ldg(mrow + (size_t)(j + 1) * mstride);
+            m2 = __ldg(mrow + (size_t)(j + 2) * mstride);
+            m3 = __ldg(mrow + (size_t)(j + 3) * mstride);
+        }
+        const float2 v0 = r32[q + j], v1 = r32[q + j + 1], v2 = r32[q + j + 2], v3 = r32[q + j + 3];
+        ar0 = fmaf(m0, v0.x, ar0); ai0 = fmaf(m0, v0.y, ai0);
+        ar1 = fmaf(m1, v1.x, ar1); ai1 = fmaf(m1, v1.y, ai1);
+        ar2 = fmaf(m2, v2.x, ar2); ai2 = fmaf(m2, v2.y, ai2);
+        ar3 = fmaf(m3, v3.x, ar3); ai3 = fmaf(m3, v3.y, ai3);
+    }
+    for (; j <= w; ++j) {
+        const float m0 = STAGE ? mrow[(size_t)j * mstride] : __ldg(mrow + (size_t)j * mstride);
+        const float2 v0 = r32[q + j];
+        ar0 = fmaf(m0, v0.x, ar0); ai0 = fmaf(m0, v0.y, ai0);
+    }
+    return make_float2((ar0 + ar1) + (ar2 + ar3), (ai0 + ai1) + (ai2 + ai3));
+}
+
+template <int KD, bool R64, bool STAGE, typename TI, typename TO, typename TV>
+__global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI* __restrict__ in,
+                                                           TO* __restrict__ out, TV* __restrict__ vstore,
+                                                           const Ctrl* __restrict__ ctrl, int dir, int scale_mode,
+                                                           int check_broken) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ unsigned s_red[kInvThreads / 32];
+    if (check_broken && ctrl->broken) return;
+    const int n = tab.n, w = tab.w, P = R64 ? tab.refine : 0;
+    const int l = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int q0 = blockIdx.x * tab.chunk;
+    int cl, R0, RB;
+    inv_region(n, q0, tab.chunk, P, w, KD, &cl, &R0, &RB);
+    const int R0p = (R0 + 3) & ~3;
+    // carve shared memory (see inv_smem_bytes)
+    unsigned char* sp = smem_raw;
+    double2* bq = reinterpret_cast<double2*>(sp);
+    sp += (size_t)RB * 16;
+    double2* xq = reinterpret_cast<double2*>(sp);
+    double2* rq = xq + R0;
+    if (R64) sp += (size_t)R0 * 16 + (size_t)RB * 16;
+    float* Ms = reinterpret_cast<float*>(sp);
+    if (STAGE) sp += (size_t)(w + 1) * R0p * 4;
+    float2* r32 = reinterpret_cast<float2*>(sp);
+
+    // stage the chunk's slice of M (float4: q0 and npad are multiples of 4)
+    const float* Mg = tab.m + q0;
+    if (STAGE) {
+        const int nv4 = R0p >> 2;
+        for (int k = tid; k < (w + 1) * nv4; k += kInvThreads) {
+            const int j = k / nv4, v = k - j * nv4;
+            reinterpret_cast<float4*>(Ms + (size_t)j * R0p)[v] =
+                __ldg(reinterpret_cast<const float4*>(Mg + (size_t)j * tab.npad) + v);
+        }
+    }
+    const double* ug = tab.u + q0;
+    const float* mbase = STAGE ? Ms : Mg;
+    const size_t mstride = STAGE ? (size_t)R0p : (size_t)tab.npad;
+    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
+    const size_t base = (size_t)l * n;
+
+    if constexpr (!R64) {
+        // plain FP32 solve (complex64 Krylov basis): x = M b
+        for (int q = tid; q < R0 + w; q += kInvThreads) {
+            float2 v = make_float2(0.f, 0.f);
+            if (q < RB) {
+                const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+                const TI t = in[base + p];
+                double2 b = make_double2((double)t.x, (double)t.y);
+                if (scale_mode) { b.x *= sc; b.y *= sc; }
+                if (vstore && q < cl) vstore[base + p] = conv<TV>(b);
+                v = make_float2((float)b.x, (float)b.y);
+            }
+            r32[q] = v;
+        }
+        __syncthreads();
+        for (int q = tid; q < cl; q += kInvThreads) {
+            const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+            out[base + p] = conv<TO>(inv_apply<STAGE>(mbase + q, mstride, r32, q, w));
+        }
+        return;
+    } else {
+    for (int q = tid; q < RB; q += kInvThreads) {
+        const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+        const TI t = in[base + p];
+        double2 b = make_double2((double)t.x, (double)t.y);
+        if (scale_mode) { b.x *= sc; b.y *= sc; }
+        if (vstore && q < cl) vstore[base + p] = conv<TV>(b);
+        bq[q] = b;
+        if (q < R0) xq[q] = make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    for (int k = 0; k <= P; ++k) {
+        const int Rk = min(n - q0, cl + (P - k) * (w + KD));
+        const int Rr = min(n - q0, Rk + w);
+        // residual r = b - U~ x (FP64) and the max of its high words (monotone in |r|)
+        unsigned hmax = 0;
+        for (int q = tid; q < Rr; q += kInvThreads) {
+            double2 r = bq[q];
+            if (k > 0) {
+#pragma unroll
+                for (int d = 0; d <= KD; ++d) {
+                    if (q + d < n - q0) {
+                        const double u = __ldg(ug + (size_t)d * n + q);
+                        r.x = fma(-u, xq[q + d].x, r.x);
+                        r.y = fma(-u, xq[q + d].y, r.y);
+                    }
+                }
+                rq[q] = r;
+            }
+            hmax = max(hmax, max((unsigned)__double2hiint(r.x) & 0x7fffffffu,
+                                 (unsigned)__double2hiint(r.y) & 0x7fffffffu));
+        }
+        hmax = __reduce_max_sync(0xffffffffu, hmax);
+        if (lane == 0) s_red[warp] = hmax;
+        __syncthreads();
+        hmax = 0;
+#pragma unroll
+        for (int i = 0; i < kInvThreads / 32; ++i) hmax = max(hmax, s_red[i]);
+        if (hmax == 0) break;                      // zero residual: x is exact (or b = 0)
+        // 2^-e brings max|r| near 1; applied only when the exponent leaves the FP32-safe range
+        const int e = (int)(hmax >> 20) - 1022;
+        const bool scaled = e < -100 || e > 100;
+        const double sdown = scaled ? ldexp(1.0, -e) : 1.0, sup = scaled ? ldexp(1.0, e) : 1.0;
+        const double2* rsrc = k > 0 ? rq : bq;
+        for (int q = tid; q < Rk + w; q += kInvThreads) {
+            float2 v = make_float2(0.f, 0.f);
+            if (q < Rr) {
+                double2 r = rsrc[q];
+                if (scaled) { r.x *= sdown; r.y *= sdown; }
+                v = make_float2((float)r.x, (float)r.y);
+            }
+            r32[q] = v;
+        }
+        __syncthreads();
+        for (int q = tid; q < Rk; q += kInvThreads) {
+            const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
+            double2 x = xq[q];
+            if (scaled) { x.x = fma((double)f.x, sup, x.x); x.y = fma((double)f.y, sup, x.y); }
+            else { x.x += (double)f.x; x.y += (double)f.y; }
+            xq[q] = x;
+        }
+        __syncthreads();
+    }
+    for (int q = tid; q < cl; q += kInvThreads) {
+        const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+        out[base + p] = conv<TO>(xq[q]);
+    }
+    }
+}
+
+template <int KD, bool R64, bool STAGE>
+static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in, int in_prec, void* out,
+                                    int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int dir,
+                                    int scale_mode, int check_broken, cudaStream_t s) {
+    const int P = R64 ? tab.refine : 0;
+    size_t smem = 0;
+    for (int c = 0; c < tab.nchunks; ++c)
+        smem = std::max(smem, inv_smem_bytes(tab.n, c * tab.chunk, tab.chunk, P, tab.w, KD, STAGE, R64));
+    dim3 grid(tab.nchunks, nrows), block(kInvThreads);
+#define GB_INV_CASE(TI_, TO_, TV_)                                                                               \
+    {                                                                                                            \
+        auto kern = k_solve_inv<KD, R64, STAGE, TI_, TO_, TV_>;                                                  \
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, dir, scale_mode,      \
+                                       check_broken);                                                            \
+        return cudaGetLastError();                                                                               \
+    }
+    // combinations the runtime uses: refined solves store double2 (or nothing), the plain
+    // FP32 solve of the mixed basis writes and stores complex64
+    const int key = in_prec * 4 + out_prec * 2 + v_prec;
+    if constexpr (R64) {
+        switch (key) {
+            case 0: GB_INV_CASE(double2, double2, double2)
+            case 2: GB_INV_CASE(double2, float2, double2)
+            case 4: GB_INV_CASE(float2, double2, double2)
+            case 6: GB_INV_CASE(float2, float2, double2)
+            default: return cudaErrorInvalidValue;
+        }
+    } else {
+        switch (key) {
+            case 3: GB_INV_CASE(double2, float2, float2)
+            case 7: GB_INV_CASE(float2, float2, float2)
+            default: return cudaErrorInvalidValue;
+        }
+    }
+#undef GB_INV_CASE
+}
+
+template <int KD>
+static cudaError_t solve_inv_kd(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
+                                int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int dir, int scale_mode,
+                                int check_broken, cudaStream_t s) {
+    if (refine64) {
+        if (tab.stage)
+            return solve_inv_launch<KD, true, true>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
+                                                    scale_mode, check_broken, s);
+        return solve_inv_launch<KD, true, false>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
+                                                 scale_mode, check_broken, s);
+    }
+    if (tab.stage)
+        return solve_inv_launch<KD, false, true>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
+                                                 scale_mode, check_broken, s);
+    return solve_inv_launch<KD, false, false>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
+                                              scale_mode, check_broken, s);
+}
+
+cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
+                             int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int dir, int scale_mode,
+                             int check_broken, cudaStream_t s) {
+    count_launch();
+    switch (tab.kd) {
+#define GB_KD(K)                                                                                                 \
+    case K:                                                                                                      \
+        return solve_inv_kd<K>(tab, nrows, refine64, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,      \
+                               scale_mode, check_broken, s);
+        GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
+#undef GB_KD
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace gbprop
