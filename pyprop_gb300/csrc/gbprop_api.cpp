@@ -237,7 +237,7 @@ struct HostInvTab {
     int n = 0, kd = 0, w = 0, npad = 0, refine = 0;
     double contraction = 0.0;          // simulated error ratio of one refinement pass
     std::vector<float> m;              // (w+1) x npad
-    std::vector<double> u;             // (kd+1) x n
+    std::vector<double> u;             // (kd+1) x npad
 };
 
 // U~ = U (dir 0) or U^T in reversed coordinates q = n-1-p (dir 1): upper triangular in q.
@@ -287,9 +287,9 @@ HostInvTab build_inv_tab(const std::vector<double>& U, int n, int kd, int dir) {
     t.m.assign((size_t)(w + 1) * t.npad, 0.0f);
     for (int j = 0; j <= w; ++j)
         for (int q = 0; q + j < n; ++q) t.m[(size_t)j * t.npad + q] = (float)inv[(size_t)j * n + q];
-    t.u.assign((size_t)(kd + 1) * n, 0.0);
+    t.u.assign((size_t)(kd + 1) * t.npad, 0.0);
     for (int d = 0; d <= kd; ++d)
-        for (int q = 0; q + d < n; ++q) t.u[(size_t)d * n + q] = ut(q, q + d);
+        for (int q = 0; q + d < n; ++q) t.u[(size_t)d * t.npad + q] = ut(q, q + d);
     // simulate the refined solve on a pseudo-random complex right-hand side
     std::vector<double> br(n), bi(n), xr(n, 0.0), xi(n, 0.0), er(n), ei(n);
     uint64_t st = 0x9e3779b97f4a7c15ull;
@@ -474,8 +474,8 @@ gbprop_status check_handle(gbprop_handle h, bool need_final) {
 // Chunking of the inverse solve.  `wide` spreads one problem's rows over the GPU: the
 // chunk count minimises (waves of CTAs) x (FP64 residual elements of one CTA, halo
 // included), the refinement being FP64-issue-bound; otherwise (batches, where other
-// problems fill the GPU) the fewest chunks are used.  The chunk's slice of M is staged
-// in shared memory when one CTA's share stays within 200 KB, else M is read through L2.
+// problems fill the GPU) the fewest chunks are used.  The chunk's slices of M and U~ are
+// staged in shared memory when one CTA's share stays within 220 KB, else read through L2.
 void set_inv_chunks(gbprop_ctx* h, bool wide) {
     const int n = h->nr, kd = h->kd, sms = grid_reduce_blocks();
     for (int dir = 0; dir < 2; ++dir) {
@@ -500,7 +500,7 @@ void set_inv_chunks(gbprop_ctx* h, bool wide) {
             for (int nch = 1; nch <= 16; ++nch) {
                 const int chunk = chunk_of(nch);
                 if (nch > 1 && chunk < 32) break;
-                if (smem_of(chunk, stage) > (size_t)200 * 1024) continue;
+                if (smem_of(chunk, stage) > (size_t)220 * 1024) continue;
                 const long c = cost(chunk);
                 if (best < 0 || (wide ? c < best_cost : false)) {
                     best = chunk;
@@ -906,6 +906,7 @@ gbprop_status gbprop_get_stats(gbprop_handle h, gbprop_stats* out) {
     out->error_estimate = c.err_est;
     if (c.lu_info) return fail(GBPROP_ELU, "Pade denominator singular (LU info " + std::to_string(c.lu_info) + ")");
     if (c.nonfinite) return fail(GBPROP_ENONFINITE, "non-finite Krylov norm");
+    if (c.wait_timeout) return fail(GBPROP_ETIMEOUT, "a bounded device wait gave up (solve table staging)");
     return GBPROP_OK;
 }
 

@@ -2,6 +2,9 @@
 #pragma once
 #include "gbprop_internal.h"
 
+#include <mutex>
+#include <unordered_set>
+
 namespace gbprop {
 
 // ---------------------------------------------------------------------------
@@ -27,6 +30,27 @@ __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+// Raise a kernel's dynamic shared-memory limit to the device's opt-in maximum, once per
+// kernel.  The limit then does not depend on which launch set it last, so graph nodes of
+// one kernel with different shared-memory sizes all stay valid, also when a tool replays
+// them one by one.
+template <typename K> inline cudaError_t allow_max_smem(K kern) {
+    static std::mutex mu;
+    static std::unordered_set<const void*> done;
+    std::lock_guard<std::mutex> lock(mu);
+    const void* key = reinterpret_cast<const void*>(kern);
+    if (done.count(key)) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kern);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess) done.insert(key);
+    return e;
 }
 
 }  // namespace gbprop

@@ -40,9 +40,10 @@ template <typename T> struct SolveTab {
 // U^-1 of a B-spline overlap factor decays geometrically away from the diagonal, so
 // w is chosen (on the host) where the dropped part is below 2^-26 of the kept one.
 //   m  (j*npad + q)  FP32, zero where q + j >= n;  npad = n rounded up to 4
-//   u  (d*n + q)     FP64, zero where q + d >= n
+//   u  (d*npad + q)  FP64, zero where q + d >= n
 // Each CTA owns `chunk` radial elements (a multiple of 4) of one row and recomputes the
-// halo its refinement passes need; stage = 1 keeps the chunk's slice of m in shared memory.
+// halo its refinement passes need; stage = 1 copies the chunk's slices of m and u into
+// shared memory with bulk asynchronous copies (16-byte aligned: q0, npad multiples of 4).
 struct InvTab {
     int n, kd, w, npad;
     int chunk, nchunks;
@@ -63,7 +64,8 @@ __host__ __device__ inline void inv_region(int n, int q0, int chunk, int P, int 
     *RB = rb < left ? rb : left;
 }
 
-// Shared-memory bytes of that CTA: b | x, r (FP64, refined solve only) | M slice (staged) | r32.
+// Shared-memory bytes of that CTA: b | x, r (FP64, refined solve only) | M slice (staged) |
+// U~ slice (staged, refined solve only) | r32.
 __host__ __device__ inline size_t inv_smem_bytes(int n, int q0, int chunk, int P, int w, int kd, int stage, int r64) {
     int cl, R0, RB;
     inv_region(n, q0, chunk, P, w, kd, &cl, &R0, &RB);
@@ -71,6 +73,7 @@ __host__ __device__ inline size_t inv_smem_bytes(int n, int q0, int chunk, int P
     size_t b = (size_t)RB * 16;
     if (r64) b += (size_t)R0 * 16 + (size_t)RB * 16;
     if (stage) b += (size_t)(w + 1) * R0p * 4;
+    if (stage && r64) b += (size_t)(kd + 1) * R0p * 8;
     b += (size_t)(R0 + w) * 8;
     return b;
 }
@@ -97,6 +100,7 @@ struct Ctrl {
     int lu_info;            // last non-zero LU info of the Pade solve
     int scaling_order;      // s of the last scaling-and-squaring
     int nonfinite;          // a NaN/Inf norm was seen
+    int wait_timeout;       // a bounded device-side wait (shared-memory staging) gave up
     int ro_go;              // re-orthogonalisation requested for the current vector
     int ro_count;           // re-orthogonalisation passes done for the current vector
     long long operator_count;
@@ -148,7 +152,7 @@ cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, cons
 // refine64 is set (FP64-accurate result); refine64 = 0 gives the plain FP32 solve of the
 // mixed path's Krylov basis.  Grid: (tab.nchunks, nrows); arguments as launch_solve.
 cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
-                             int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int dir, int scale_mode,
+                             int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
                              int check_broken, cudaStream_t s);
 cudaError_t launch_band_apply(int arith, const void* op, const void* x, void* y, const SchedEntry* sched,
                               const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s);

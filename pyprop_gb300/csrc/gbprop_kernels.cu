@@ -1168,7 +1168,7 @@ template <int CL>
 static cudaError_t launch_expm_cl(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s) {
     const size_t smem = (size_t)7 * m * m * sizeof(double2);
     auto kern = k_expm_cluster<CL>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_smem(kern);
     if (e != cudaSuccess) return e;
     if (CL > 8) {
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -1193,7 +1193,7 @@ template <int CL>
 static bool cluster_fits(int m) {
     const size_t smem = (size_t)7 * m * m * sizeof(double2);
     auto kern = k_expm_cluster<CL>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return false;
+    if (allow_max_smem(kern) != cudaSuccess) return false;
     if (CL > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
         return false;
     cudaLaunchConfig_t cfg = {};
@@ -1229,7 +1229,10 @@ cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, i
     if (cl == 16 && max_cluster >= 16) return launch_expm_cl<16>(ctrl, H, m, sched, s);
     if (cl == 8) return launch_expm_cl<8>(ctrl, H, m, sched, s);
     const size_t smem = (size_t)5 * m * m * sizeof(double2);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 48 * 1024) {
+        cudaError_t e = allow_max_smem(k_expm);
+        if (e != cudaSuccess) return e;
+    }
     k_expm<<<1, 256, smem, s>>>(ctrl, H, m, sched);
     return cudaGetLastError();
 }

@@ -263,7 +263,10 @@ static cudaError_t solve_kd(const SolveTab<T>& tab, int nrows, const void* in, i
 #define GB_SOLVE_CASE(TI_, TO_, TV_)                                                                             \
     {                                                                                                            \
         auto kern = k_solve<T, KD, TI_, TO_, TV_>;                                                               \
-        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        if (smem > 48 * 1024) {                                                                                  \
+            cudaError_t ea = allow_max_smem(kern);                                                               \
+            if (ea != cudaSuccess) return ea;                                                                    \
+        }                                                                                                        \
         kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,           \
                                        check_broken);                                                            \
         return cudaGetLastError();                                                                               \
@@ -319,7 +322,10 @@ static cudaError_t solve_ir_kd(const SolveTab<float>& tab, const double* udp, in
 #define GB_IR_CASE(TI_, TO_, TV_)                                                                                \
     {                                                                                                            \
         auto kern = k_solve_ir<KD, TI_, TO_, TV_>;                                                               \
-        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        if (smem > 48 * 1024) {                                                                                  \
+            cudaError_t ea = allow_max_smem(kern);                                                               \
+            if (ea != cudaSuccess) return ea;                                                                    \
+        }                                                                                                        \
         kern<<<grid, block, smem, s>>>(tab, udp, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, scale_mode,      \
                                        check_broken, stage_tables, stage_udp);                                   \
         return cudaGetLastError();                                                                               \
@@ -356,12 +362,38 @@ cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, cons
 // CTA (chunk c, row l) produces x on q in [q0, q0 + cl), q0 = c * chunk.  With P
 // refinement passes, pass k (0..P) updates x on [q0, q0 + R_k), R_k = cl + (P-k)(w+kd):
 //     r = b - U~ x          (FP64; pass 0: r = b, x = 0)
-//     x += 2^e * M (2^-e r) (FP32 products and sums; 2^-e scales max|r| below 1)
+//     x += 2^e * M (2^-e r) (FP32 products and sums; 2^-e only when max|r| leaves the
+//                            comfortable FP32 exponent range)
 // x on R_k needs r on R_k + w, which needs the previous x on R_k + w + kd = R_{k-1}, so
 // the chunk's halo is recomputed instead of exchanged.  Every element of the region is
-// independent inside a pass: one thread per element, two barriers per pass.
-constexpr int kInvThreads = 256;
+// independent inside a pass: one thread per element, two barriers per pass.  The chunk's
+// slices of M and U~ arrive by bulk asynchronous copies (one mbarrier) while the threads
+// load the right-hand side.
+constexpr int kInvThreads = 512;
+constexpr long kInvWaitLimit = 1L << 24;      // try_wait polls before a staging wait gives up
 
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+// Bounded wait for phase 0 of the mbarrier; false when the poll limit was reached.
+__device__ __forceinline__ bool mbar_wait0(unsigned long long* bar) {
+    const unsigned a = smem_u32(bar);
+    for (long it = 0; it < kInvWaitLimit; ++it) {
+        unsigned done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+                     " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(a) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// x (+)= M r32 for element q: FP32 products, four independent chains per component.
 template <bool STAGE>
 __device__ __forceinline__ float2 inv_apply(const float* mrow, size_t mstride, const float2* r32, int q, int w) {
     float ar0 = 0.f, ai0 = 0.f, ar1 = 0.f, ai1 = 0.f, ar2 = 0.f, ai2 = 0.f, ar3 = 0.f, ai3 = 0.f;
@@ -396,10 +428,11 @@ __device__ __forceinline__ float2 inv_apply(const float* mrow, size_t mstride, c
 template <int KD, bool R64, bool STAGE, typename TI, typename TO, typename TV>
 __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI* __restrict__ in,
                                                            TO* __restrict__ out, TV* __restrict__ vstore,
-                                                           const Ctrl* __restrict__ ctrl, int dir, int scale_mode,
+                                                           Ctrl* __restrict__ ctrl, int dir, int scale_mode,
                                                            int check_broken) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ unsigned s_red[kInvThreads / 32];
+    __shared__ __align__(8) unsigned long long s_bar;
     if (check_broken && ctrl->broken) return;
     const int n = tab.n, w = tab.w, P = R64 ? tab.refine : 0;
     const int l = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -416,21 +449,34 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
     if (R64) sp += (size_t)R0 * 16 + (size_t)RB * 16;
     float* Ms = reinterpret_cast<float*>(sp);
     if (STAGE) sp += (size_t)(w + 1) * R0p * 4;
+    double* Us = reinterpret_cast<double*>(sp);
+    if (STAGE && R64) sp += (size_t)(KD + 1) * R0p * 8;
     float2* r32 = reinterpret_cast<float2*>(sp);
 
-    // stage the chunk's slice of M (float4: q0 and npad are multiples of 4)
     const float* Mg = tab.m + q0;
+    const double* Ug = tab.u + q0;
     if (STAGE) {
-        const int nv4 = R0p >> 2;
-        for (int k = tid; k < (w + 1) * nv4; k += kInvThreads) {
-            const int j = k / nv4, v = k - j * nv4;
-            reinterpret_cast<float4*>(Ms + (size_t)j * R0p)[v] =
-                __ldg(reinterpret_cast<const float4*>(Mg + (size_t)j * tab.npad) + v);
+        // one thread arms the barrier with the byte count and issues one bulk copy per
+        // diagonal (rows of R0p elements: sizes and addresses are multiples of 16 bytes)
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&s_bar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();                               // barrier initialised before anyone polls it
+        if (tid == 0) {
+            const unsigned mrow = (unsigned)R0p * 4, urow = (unsigned)R0p * 8;
+            const unsigned bytes = (unsigned)(w + 1) * mrow + (R64 ? (unsigned)(KD + 1) * urow : 0u);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         :: "r"(smem_u32(&s_bar)), "r"(bytes) : "memory");
+            for (int j = 0; j <= w; ++j) bulk_g2s(Ms + (size_t)j * R0p, Mg + (size_t)j * tab.npad, mrow, &s_bar);
+            if (R64)
+                for (int d = 0; d <= KD; ++d) bulk_g2s(Us + (size_t)d * R0p, Ug + (size_t)d * tab.npad, urow, &s_bar);
         }
     }
-    const double* ug = tab.u + q0;
     const float* mbase = STAGE ? Ms : Mg;
     const size_t mstride = STAGE ? (size_t)R0p : (size_t)tab.npad;
+    const double* ubase = STAGE ? Us : Ug;
+    const size_t ustride = STAGE ? (size_t)R0p : (size_t)tab.npad;
     const double sc = scale_mode ? ctrl->inv_beta : 1.0;
     const size_t base = (size_t)l * n;
 
@@ -448,85 +494,101 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
             }
             r32[q] = v;
         }
-        __syncthreads();
+        bool ok = true;
+        if (STAGE) ok = mbar_wait0(&s_bar);
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) ctrl->wait_timeout = 1;
+            if (STAGE) mbar_wait0(&s_bar);             // let copies in flight land before exit
+            return;
+        }
         for (int q = tid; q < cl; q += kInvThreads) {
             const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
             out[base + p] = conv<TO>(inv_apply<STAGE>(mbase + q, mstride, r32, q, w));
         }
         return;
     } else {
-    for (int q = tid; q < RB; q += kInvThreads) {
-        const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-        const TI t = in[base + p];
-        double2 b = make_double2((double)t.x, (double)t.y);
-        if (scale_mode) { b.x *= sc; b.y *= sc; }
-        if (vstore && q < cl) vstore[base + p] = conv<TV>(b);
-        bq[q] = b;
-        if (q < R0) xq[q] = make_double2(0.0, 0.0);
-    }
-    __syncthreads();
-    for (int k = 0; k <= P; ++k) {
-        const int Rk = min(n - q0, cl + (P - k) * (w + KD));
-        const int Rr = min(n - q0, Rk + w);
-        // residual r = b - U~ x (FP64) and the max of its high words (monotone in |r|)
-        unsigned hmax = 0;
-        for (int q = tid; q < Rr; q += kInvThreads) {
-            double2 r = bq[q];
-            if (k > 0) {
+        for (int q = tid; q < RB; q += kInvThreads) {
+            const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+            const TI t = in[base + p];
+            double2 b = make_double2((double)t.x, (double)t.y);
+            if (scale_mode) { b.x *= sc; b.y *= sc; }
+            if (vstore && q < cl) vstore[base + p] = conv<TV>(b);
+            bq[q] = b;
+            if (q < R0) xq[q] = make_double2(0.0, 0.0);
+        }
+        bool ok = true;
+        if (STAGE) ok = mbar_wait0(&s_bar);
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) ctrl->wait_timeout = 1;
+            if (STAGE) mbar_wait0(&s_bar);
+            return;
+        }
+        for (int k = 0; k <= P; ++k) {
+            const int Rk = min(n - q0, cl + (P - k) * (w + KD));
+            const int Rr = min(n - q0, Rk + w);
+            // residual r = b - U~ x (FP64, two FMA chains per component) and the max of
+            // its high words (monotone in |r|)
+            unsigned hmax = 0;
+            for (int q = tid; q < Rr; q += kInvThreads) {
+                double2 r = bq[q];
+                if (k > 0) {
+                    double ar = 0.0, ai = 0.0;
 #pragma unroll
-                for (int d = 0; d <= KD; ++d) {
-                    if (q + d < n - q0) {
-                        const double u = __ldg(ug + (size_t)d * n + q);
-                        r.x = fma(-u, xq[q + d].x, r.x);
-                        r.y = fma(-u, xq[q + d].y, r.y);
+                    for (int d = 0; d <= KD; ++d) {
+                        if (q + d < n - q0) {
+                            const double u = ubase[(size_t)d * ustride + q];
+                            const double2 xv = xq[q + d];
+                            if (d & 1) { ar = fma(-u, xv.x, ar); ai = fma(-u, xv.y, ai); }
+                            else { r.x = fma(-u, xv.x, r.x); r.y = fma(-u, xv.y, r.y); }
+                        }
                     }
+                    r.x += ar;
+                    r.y += ai;
+                    rq[q] = r;
                 }
-                rq[q] = r;
+                hmax = max(hmax, max((unsigned)__double2hiint(r.x) & 0x7fffffffu,
+                                     (unsigned)__double2hiint(r.y) & 0x7fffffffu));
             }
-            hmax = max(hmax, max((unsigned)__double2hiint(r.x) & 0x7fffffffu,
-                                 (unsigned)__double2hiint(r.y) & 0x7fffffffu));
-        }
-        hmax = __reduce_max_sync(0xffffffffu, hmax);
-        if (lane == 0) s_red[warp] = hmax;
-        __syncthreads();
-        hmax = 0;
+            hmax = __reduce_max_sync(0xffffffffu, hmax);
+            if (lane == 0) s_red[warp] = hmax;
+            __syncthreads();
+            hmax = 0;
 #pragma unroll
-        for (int i = 0; i < kInvThreads / 32; ++i) hmax = max(hmax, s_red[i]);
-        if (hmax == 0) break;                      // zero residual: x is exact (or b = 0)
-        // 2^-e brings max|r| near 1; applied only when the exponent leaves the FP32-safe range
-        const int e = (int)(hmax >> 20) - 1022;
-        const bool scaled = e < -100 || e > 100;
-        const double sdown = scaled ? ldexp(1.0, -e) : 1.0, sup = scaled ? ldexp(1.0, e) : 1.0;
-        const double2* rsrc = k > 0 ? rq : bq;
-        for (int q = tid; q < Rk + w; q += kInvThreads) {
-            float2 v = make_float2(0.f, 0.f);
-            if (q < Rr) {
-                double2 r = rsrc[q];
-                if (scaled) { r.x *= sdown; r.y *= sdown; }
-                v = make_float2((float)r.x, (float)r.y);
+            for (int i = 0; i < kInvThreads / 32; ++i) hmax = max(hmax, s_red[i]);
+            if (hmax == 0) break;                      // zero residual: x is exact (or b = 0)
+            const int e = (int)(hmax >> 20) - 1022;
+            const bool scaled = e < -100 || e > 100;
+            const double sdown = scaled ? ldexp(1.0, -e) : 1.0, sup = scaled ? ldexp(1.0, e) : 1.0;
+            const double2* rsrc = k > 0 ? rq : bq;
+            for (int q = tid; q < Rk + w; q += kInvThreads) {
+                float2 v = make_float2(0.f, 0.f);
+                if (q < Rr) {
+                    double2 r = rsrc[q];
+                    if (scaled) { r.x *= sdown; r.y *= sdown; }
+                    v = make_float2((float)r.x, (float)r.y);
+                }
+                r32[q] = v;
             }
-            r32[q] = v;
+            __syncthreads();
+            for (int q = tid; q < Rk; q += kInvThreads) {
+                const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
+                double2 x = xq[q];
+                if (scaled) { x.x = fma((double)f.x, sup, x.x); x.y = fma((double)f.y, sup, x.y); }
+                else { x.x += (double)f.x; x.y += (double)f.y; }
+                xq[q] = x;
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        for (int q = tid; q < Rk; q += kInvThreads) {
-            const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
-            double2 x = xq[q];
-            if (scaled) { x.x = fma((double)f.x, sup, x.x); x.y = fma((double)f.y, sup, x.y); }
-            else { x.x += (double)f.x; x.y += (double)f.y; }
-            xq[q] = x;
+        for (int q = tid; q < cl; q += kInvThreads) {
+            const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+            out[base + p] = conv<TO>(xq[q]);
         }
-        __syncthreads();
-    }
-    for (int q = tid; q < cl; q += kInvThreads) {
-        const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-        out[base + p] = conv<TO>(xq[q]);
-    }
     }
 }
 
 template <int KD, bool R64, bool STAGE>
 static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in, int in_prec, void* out,
-                                    int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int dir,
+                                    int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir,
                                     int scale_mode, int check_broken, cudaStream_t s) {
     const int P = R64 ? tab.refine : 0;
     size_t smem = 0;
@@ -536,7 +598,10 @@ static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in
 #define GB_INV_CASE(TI_, TO_, TV_)                                                                               \
     {                                                                                                            \
         auto kern = k_solve_inv<KD, R64, STAGE, TI_, TO_, TV_>;                                                  \
-        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        if (smem > 48 * 1024) {                                                                                  \
+            cudaError_t ea = allow_max_smem(kern);                                                               \
+            if (ea != cudaSuccess) return ea;                                                                    \
+        }                                                                                                        \
         kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, dir, scale_mode,      \
                                        check_broken);                                                            \
         return cudaGetLastError();                                                                               \
@@ -564,7 +629,7 @@ static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in
 
 template <int KD>
 static cudaError_t solve_inv_kd(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
-                                int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int dir, int scale_mode,
+                                int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
                                 int check_broken, cudaStream_t s) {
     if (refine64) {
         if (tab.stage)
@@ -581,7 +646,7 @@ static cudaError_t solve_inv_kd(const InvTab& tab, int nrows, int refine64, cons
 }
 
 cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
-                             int out_prec, void* vstore, int v_prec, const Ctrl* ctrl, int dir, int scale_mode,
+                             int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
                              int check_broken, cudaStream_t s) {
     count_launch();
     switch (tab.kd) {
