@@ -49,27 +49,10 @@ def hat_weights(times, T, nsamples):
 
 
 def bound_states(problem, emax=0.0, lmax_states=None):
-    """Bound eigenstates (E < emax) of the field-free Hamiltonian, per l, as physical
-    coefficient vectors phi_b (nl*nr) normalised in the overlap metric, and energies."""
-    import scipy.linalg as sl
-    from .tensorpotential import bandnh_to_dense
-    nl, nr, kb = problem.nl, problem.nr, problem.kb
-    S = np.zeros((nr, nr))
-    for d in range(-problem.kd, problem.kd + 1):
-        i = np.arange(max(0, -d), min(nr, nr - d))
-        S[i, i + d] = problem.Sdiag[problem.kd + d, i]
-    states, energies, ls = [], [], []
-    for l in range(nl if lmax_states is None else min(nl, lmax_states + 1)):
-        H = bandnh_to_dense(problem.static[l], nr, kb).real
-        H = 0.5 * (H + H.T)
-        e, v = sl.eigh(H, S)
-        for j in np.where(e < emax)[0]:
-            phi = np.zeros((nl, nr), dtype=np.complex128)
-            phi[l] = v[:, j] / math.sqrt(v[:, j] @ S @ v[:, j])
-            states.append(phi.ravel())
-            energies.append(e[j])
-            ls.append(l)
-    return np.array(states), np.array(energies), np.array(ls)
+    """Bound eigenstates (E < emax) of a batch.HydrogenProblem's field-free Hamiltonian, per l,
+    S-normalised physical coefficient vectors (observables.hydrogen_bound_states)."""
+    from .observables import hydrogen_bound_states
+    return hydrogen_bound_states(problem, emax, lmax_states)
 
 
 class AugmentedOperator:

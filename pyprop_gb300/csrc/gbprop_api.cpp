@@ -96,10 +96,10 @@ struct gbprop_ctx {
     void* d_s = nullptr;              // N, Krylov precision (U^-1 v)
     void* d_y = nullptr;              // N, Krylov precision (H U^-1 v)
     double2* d_x = nullptr;           // N, complex128 (U psi, V y)
+    double2* d_v0 = nullptr;          // N, complex128 first basis vector of a complex64 basis
     std::vector<void*> allocs;
 
-    cudaGraphExec_t graph = nullptr;
-    const void* graph_psi = nullptr;
+    cudaGraphExec_t graph = nullptr;      // one step on x (independent of the caller's buffers)
     long long graph_launches = 0;
     int band_variant = 1;             // tile shape of the band kernel (autotuner)
     int expm_max_cluster = 16;        // 1 when the handle is advanced inside a batch
@@ -456,6 +456,16 @@ gbprop_status upload_band_op(gbprop_ctx* h, const HostBandOp& ho, BandOp<T>* out
     out->t_timedep = td;
     out->t_coef = coef;
     out->slots = slots;
+    out->slots_lo = nullptr;
+    if (sizeof(T) < sizeof(double)) {
+        // complex64 path: the rounding remainder of every coefficient, so the operator
+        // applied is the FP64 one (to ~2^-48) and only the FP32 sums round
+        std::vector<T> lo(sl.size());
+        for (size_t k = 0; k < sl.size(); ++k) lo[k] = (T)(k < ho.slots.size() ? ho.slots[k] - (double)sl[k] : 0.0);
+        T* dlo;
+        if ((st = h->upload(&dlo, lo))) return st;
+        out->slots_lo = dlo;
+    }
     return GBPROP_OK;
 }
 
@@ -544,8 +554,28 @@ const void* kop(gbprop_ctx* h) {
     return h->prec == GBPROP_FP64 ? (const void*)&h->t64.op : (const void*)&h->t32.op;
 }
 
-// Enqueue one AdvanceStep (PamPropagator.py:50-57 around pamp.h:613-669).
-gbprop_status enqueue_step(gbprop_ctx* h, void* psi) {
+// The state lives in FP64 balanced coordinates x = U psi (MultiplySqrtOverlap,
+// PamPropagator.py:50-52) for the whole of one advance call: enter() forms it, every
+// step maps x to x (pamp.h:613-669), leave() returns psi = U^-1 x (SolveSqrtOverlap,
+// PamPropagator.py:55-57).  Per step the reference's R^-1 R round trip is exact
+// algebra; keeping x removes its rounding and, for complex64 wavefunctions, the
+// per-step rounding of the state.
+gbprop_status enqueue_enter(gbprop_ctx* h, void* psi, cudaStream_t s) {
+    GB_LAUNCH(launch_tbmv(0, h->kd, h->d_ud_phys, h->nl, h->nr, psi, h->kprec(), h->d_x, 0, s));
+    return GBPROP_OK;
+}
+
+gbprop_status enqueue_leave(gbprop_ctx* h, void* psi, cudaStream_t s) {
+    cudaStream_t keep = h->stream;
+    h->stream = s;
+    cudaError_t e = ssolve(h, 0, h->d_x, 0, psi, h->kprec());
+    h->stream = keep;
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("ssolve: ") + cudaGetErrorString(e));
+    return GBPROP_OK;
+}
+
+// Enqueue one AdvanceStep on x (PamPropagator.py:50-57 around pamp.h:613-669).
+gbprop_status enqueue_step(gbprop_ctx* h) {
     cudaStream_t s = h->stream;
     const int kp = h->kprec();
     const int m = h->m;
@@ -553,35 +583,39 @@ gbprop_status enqueue_step(gbprop_ctx* h, void* psi) {
     char* V = (char*)h->d_V;
     const size_t vbytes = (size_t)N * h->kelem();
     GB_LAUNCH(launch_step_begin(h->d_ctrl, h->d_H, m, s));
-    // psi <- U psi (MultiplySqrtOverlap(false)), kept in complex128, and beta0 = ||U psi||
-    GB_LAUNCH(launch_tbmv(0, h->kd, h->d_ud_phys, h->nl, h->nr, psi, kp, h->d_x, 0, s));
+    // beta0 = ||x||
     GB_LAUNCH(launch_norm(0, h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
     for (int J = 0; J < m; ++J) {
         const void* in = J == 0 ? (const void*)h->d_x : (const void*)h->d_r;
         const int in_prec = J == 0 ? 0 : kp;
-        // v_J = r / beta_J stored in V[J]; s = U^-1 v_J
-        GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1));
+        // v_J = r / beta_J stored in V[J] (v_0 of a complex64 basis in FP64); s = U^-1 v_J
+        if (J == 0 && h->d_v0)
+            GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, h->d_v0, 0, 1, 1));
+        else
+            GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1));
         // y = sum_t c_t s_t A_t s
         GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, h->d_sched, h->d_ctrl, 0.0, 1, s));
         // w = U^-T y
         GB_LAUNCH(ksolve(h, 1, h->d_y, kp, h->d_r, kp, nullptr, kp, 0, 1));
         // classical Gram-Schmidt against v_0..v_J
-        GB_LAUNCH(launch_cgs_dot(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0, h->double_orth, s));
+        GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0,
+                                 h->double_orth, s));
         if (J < m - 1 || h->double_orth)
-            GB_LAUNCH(launch_cgs_update(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl,
+            GB_LAUNCH(launch_cgs_update(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl,
                                         h->double_orth ? 2 : 0, s));
         if (h->double_orth) {
             for (int pass = 0; pass < 3; ++pass) {
-                GB_LAUNCH(launch_cgs_dot(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, 0, s));
-                GB_LAUNCH(launch_cgs_update(kp, V, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, s));
+                GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, 0,
+                                         s));
+                GB_LAUNCH(launch_cgs_update(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1,
+                                            s));
             }
         }
         GB_LAUNCH(launch_arnoldi_finalize(h->d_ctrl, h->d_H, m, J, h->double_orth, s));
     }
     GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s));
-    GB_LAUNCH(launch_combine(kp, V, N, h->d_ctrl, h->d_x, s));
-    // psi <- U^-1 (beta0 V y)  (SolveSqrtOverlap(false))
-    GB_LAUNCH(ssolve(h, 0, h->d_x, 0, psi, kp));
+    // x <- beta0 V exp(-i dt H) e1
+    GB_LAUNCH(launch_combine(kp, V, h->d_v0, N, h->d_ctrl, h->d_x, s));
     GB_LAUNCH(launch_step_end(h->d_ctrl, s));
     return GBPROP_OK;
 }
@@ -590,7 +624,6 @@ void drop_graph(gbprop_ctx* h) {
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
-        h->graph_psi = nullptr;
     }
 }
 
@@ -601,16 +634,12 @@ void set_band_variant(gbprop_ctx* h, int v) {
     drop_graph(h);
 }
 
-gbprop_status ensure_graph(gbprop_ctx* h, void* psi) {
-    if (h->graph && h->graph_psi == psi) return GBPROP_OK;
-    if (h->graph) {
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
-    }
+gbprop_status ensure_graph(gbprop_ctx* h) {
+    if (h->graph) return GBPROP_OK;
     cudaGraph_t g = nullptr;
     GB_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     const long long before = launch_count();
-    gbprop_status st = enqueue_step(h, psi);
+    gbprop_status st = enqueue_step(h);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (st) {
         if (g) cudaGraphDestroy(g);
@@ -623,7 +652,6 @@ gbprop_status ensure_graph(gbprop_ctx* h, void* psi) {
     e = cudaGraphInstantiate(&h->graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-    h->graph_psi = psi;
     return GBPROP_OK;
 }
 
@@ -637,11 +665,7 @@ gbprop_status ensure_sched(gbprop_ctx* h, int n) {
     if (st) return st;
     h->d_sched = p;
     h->sched_cap = cap;
-    if (h->graph) {
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
-        h->graph_psi = nullptr;
-    }
+    drop_graph(h);
     return GBPROP_OK;
 }
 
@@ -762,12 +786,21 @@ gbprop_status gbprop_finalize(gbprop_handle h) {
                 t.w = hi[dir].w;
                 t.npad = hi[dir].npad;
                 t.refine = std::max(hi[0].refine, hi[1].refine);
-                float* dm;
+                float *dm, *duh, *dul;
                 double* du;
+                std::vector<float> uh(hi[dir].u.size()), ul(hi[dir].u.size());
+                for (size_t k = 0; k < uh.size(); ++k) {
+                    uh[k] = (float)hi[dir].u[k];
+                    ul[k] = (float)(hi[dir].u[k] - (double)uh[k]);
+                }
                 if ((st = h->upload(&dm, hi[dir].m))) return st;
                 if ((st = h->upload(&du, hi[dir].u))) return st;
+                if ((st = h->upload(&duh, uh))) return st;
+                if ((st = h->upload(&dul, ul))) return st;
                 t.m = dm;
                 t.u = du;
+                t.uh = duh;
+                t.ul = dul;
             }
             set_inv_chunks(h, true);
             h->inv_ok = true;
@@ -797,6 +830,7 @@ gbprop_status gbprop_finalize(gbprop_handle h) {
     if ((st = h->dalloc(&h->d_s, (size_t)h->N * ke))) return st;
     if ((st = h->dalloc(&h->d_y, (size_t)h->N * ke))) return st;
     if ((st = h->dalloc(&h->d_x, (size_t)h->N * sizeof(double2)))) return st;
+    if (h->prec != GBPROP_FP64 && (st = h->dalloc(&h->d_v0, (size_t)h->N * sizeof(double2)))) return st;
     if ((st = ensure_sched(h, 1024))) return st;
     GB_CUDA(cudaStreamSynchronize(h->stream));
     h->finalized = true;
@@ -812,6 +846,7 @@ gbprop_status gbprop_advance(gbprop_handle h, void* psi, int nsteps, const doubl
     if (!scalings) return fail(GBPROP_EINVAL, "null scaling schedule");
     gbprop_status st;
     GB_CUDA(h->begin());
+    if ((st = enqueue_enter(h, psi, h->stream))) return st;
     // steps are issued in chunks of the schedule capacity
     int done = 0;
     while (done < nsteps) {
@@ -822,13 +857,14 @@ gbprop_status gbprop_advance(gbprop_handle h, void* psi, int nsteps, const doubl
         // pageable source: staged before the call returns, so `sched` may go out of scope
         GB_CUDA(cudaMemcpyAsync(h->d_sched, sched.data(), chunk * sizeof(SchedEntry), cudaMemcpyHostToDevice, h->stream));
         GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), h->stream));
-        if ((st = ensure_graph(h, psi))) return st;
+        if ((st = ensure_graph(h))) return st;
         for (int k = 0; k < chunk; ++k) {
             GB_CUDA(cudaGraphLaunch(h->graph, h->stream));
             count_launch((int)h->graph_launches);
         }
         done += chunk;
     }
+    if ((st = enqueue_leave(h, psi, h->stream))) return st;
     GB_CUDA(h->end());
     return GBPROP_OK;
 }
@@ -1013,11 +1049,14 @@ struct gbprop_batch_ctx {
     cudaStream_t stream = nullptr, ustream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_in = nullptr, ev_out = nullptr;
     std::vector<cudaEvent_t> ev_join;
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;                  // one step of every problem
+    cudaGraphExec_t g_enter = nullptr, g_leave = nullptr;   // x = U psi / psi = U^-1 x of every problem
     std::vector<void*> graph_psi;
-    long long graph_launches = 0;
+    long long graph_launches = 0, enter_launches = 0, leave_launches = 0;
     ~gbprop_batch_ctx() {
         if (graph) cudaGraphExecDestroy(graph);
+        if (g_enter) cudaGraphExecDestroy(g_enter);
+        if (g_leave) cudaGraphExecDestroy(g_leave);
         for (cudaEvent_t e : ev_join) cudaEventDestroy(e);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_in) cudaEventDestroy(ev_in);
@@ -1028,10 +1067,12 @@ struct gbprop_batch_ctx {
 
 namespace {
 
-gbprop_status batch_capture(gbprop_batch b, void* const* psi) {
-    if (b->graph) {
-        cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
+// Capture one parallel branch per problem (forked from and joined into the batch stream).
+// what: 0 = one step, 1 = enter (x = U psi), 2 = leave (psi = U^-1 x).
+gbprop_status batch_capture(gbprop_batch b, void* const* psi, int what, cudaGraphExec_t* out, long long* launches) {
+    if (*out) {
+        cudaGraphExecDestroy(*out);
+        *out = nullptr;
     }
     cudaGraph_t g = nullptr;
     GB_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -1042,7 +1083,8 @@ gbprop_status batch_capture(gbprop_batch b, void* const* psi) {
         gbprop_ctx* h = b->hs[p];
         e = cudaStreamWaitEvent(h->stream, b->ev_fork, 0);
         if (e != cudaSuccess) break;
-        st = enqueue_step(h, psi[p]);
+        st = what == 0 ? enqueue_step(h) : what == 1 ? enqueue_enter(h, psi[p], h->stream)
+                                                     : enqueue_leave(h, psi[p], h->stream);
         if (st) break;
         e = cudaEventRecord(b->ev_join[p], h->stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_join[p], 0);
@@ -1056,12 +1098,11 @@ gbprop_status batch_capture(gbprop_batch b, void* const* psi) {
         if (g) cudaGraphDestroy(g);
         return fail(GBPROP_ECUDA, std::string("batch capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
     }
-    b->graph_launches = launch_count() - before;
-    count_launch((int)-b->graph_launches);
-    e = cudaGraphInstantiate(&b->graph, g, 0);
+    *launches = launch_count() - before;
+    count_launch((int)-*launches);
+    e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-    b->graph_psi.assign(psi, psi + b->hs.size());
     return GBPROP_OK;
 }
 
@@ -1120,6 +1161,16 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
         if (!psi[p]) return fail(GBPROP_EINVAL, "null wavefunction in batch");
     GB_CUDA(cudaEventRecord(b->ev_in, b->ustream));
     GB_CUDA(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
+    bool new_psi = b->graph_psi.size() != P || !b->g_enter || !b->g_leave;
+    for (size_t p = 0; p < P && !new_psi; ++p)
+        if (b->graph_psi[p] != psi[p]) new_psi = true;
+    if (new_psi) {
+        if (gbprop_status st = batch_capture(b, psi, 1, &b->g_enter, &b->enter_launches)) return st;
+        if (gbprop_status st = batch_capture(b, psi, 2, &b->g_leave, &b->leave_launches)) return st;
+        b->graph_psi.assign(psi, psi + P);
+    }
+    GB_CUDA(cudaGraphLaunch(b->g_enter, b->stream));
+    count_launch((int)b->enter_launches);
     int done = 0;
     while (done < nsteps) {
         int cap = 1 << 30;
@@ -1138,16 +1189,16 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
                                     b->stream));
             GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), b->stream));
         }
-        for (size_t p = 0; p < P && !recapture; ++p)
-            if (b->graph_psi[p] != psi[p]) recapture = true;
         if (recapture)
-            if (gbprop_status st = batch_capture(b, psi)) return st;
+            if (gbprop_status st = batch_capture(b, psi, 0, &b->graph, &b->graph_launches)) return st;
         for (int k = 0; k < chunk; ++k) {
             GB_CUDA(cudaGraphLaunch(b->graph, b->stream));
             count_launch((int)b->graph_launches);
         }
         done += chunk;
     }
+    GB_CUDA(cudaGraphLaunch(b->g_leave, b->stream));
+    count_launch((int)b->leave_launches);
     GB_CUDA(cudaEventRecord(b->ev_out, b->stream));
     GB_CUDA(cudaStreamWaitEvent(b->ustream, b->ev_out, 0));
     return GBPROP_OK;

@@ -32,6 +32,31 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// Error-free transformations in FP32 (no contraction: explicit round-to-nearest ops).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// acc (hi, lo) += (uh + ul) * x, with uh*x split exactly into product and rounding error.
+__device__ __forceinline__ void acc_prod(float& hi, float& lo, float uh, float ul, float x) {
+    const float p = __fmul_rn(uh, x);
+    const float pe = __fmaf_rn(uh, x, -p);
+    float t;
+    two_sum(hi, p, hi, t);
+    lo = __fadd_rn(lo, __fadd_rn(t, __fmaf_rn(ul, x, pe)));
+}
+
+// (hi, lo) += (ch + cl) * (sh + sl), first order in the low parts.
+__device__ __forceinline__ void acc_scaled(float& hi, float& lo, float ch, float cl, float sh, float sl) {
+    const float p = __fmul_rn(ch, sh);
+    const float pe = __fmaf_rn(ch, sh, -p);
+    float t;
+    two_sum(hi, p, hi, t);
+    lo = __fadd_rn(lo, __fadd_rn(t, __fadd_rn(pe, __fmaf_rn(ch, sl, __fmul_rn(cl, sh)))));
+}
+
 // Raise a kernel's dynamic shared-memory limit to the device's opt-in maximum, once per
 // kernel.  The limit then does not depend on which launch set it last, so graph nodes of
 // one kernel with different shared-memory sizes all stay valid, also when a tool replays

@@ -51,6 +51,8 @@ struct InvTab {
     int stage;
     const float* m;
     const double* u;
+    const float* uh;        // u split into FP32 pairs u = uh + ul (same layout), for the
+    const float* ul;        // error-free residual of the complex64 solve
 };
 
 // Region of the CTA whose chunk starts at q0, for P refinement passes: cl elements written,
@@ -78,6 +80,18 @@ __host__ __device__ inline size_t inv_smem_bytes(int n, int q0, int chunk, int P
     return b;
 }
 
+// Shared memory of the complex64 (mixed-path) solve with one refinement:
+// M slice | uh, ul slices (staged) | b hi, b lo | x0 | r32.
+__host__ __device__ inline size_t inv_smem_bytes_mixed(int n, int q0, int chunk, int w, int kd, int stage) {
+    int cl, R0, RB;
+    inv_region(n, q0, chunk, 1, w, kd, &cl, &R0, &RB);
+    const int R0p = (R0 + 3) & ~3;
+    size_t b = 0;
+    if (stage) b += (size_t)(w + 1) * R0p * 4 + (size_t)2 * (kd + 1) * R0p * 4;
+    b += (size_t)RB * 16 + (size_t)R0 * 8 + (size_t)(R0 + w) * 8;
+    return b;
+}
+
 // Term list of the tensor-potential matvec, grouped by destination row l:
 //   y[l][i] += coef_t * s_t * sum_d slot[t][d][i] * x[src_t][i + d - kb]
 // slots are real bands stored diagonal-major: (slot*(2kb+1) + d)*nr + i = A(i, i+d-kb).
@@ -90,6 +104,7 @@ template <typename T> struct BandOp {
     const int* t_timedep;    // nterms
     const double* t_coef;    // 2 * nterms (re, im)
     const T* slots;
+    const T* slots_lo;       // FP32 only: slot - (float)slot, the coefficients' rounding remainder
 };
 
 // Device control block of one handle; every field is written by kernels only.
@@ -149,8 +164,9 @@ cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, cons
                             cudaStream_t s);
 // Solve through the banded approximate inverse of the overlap factor (see InvTab):
 // x = M b in FP32, then `refine` passes x += M (b - U~ x) with FP64 residuals when
-// refine64 is set (FP64-accurate result); refine64 = 0 gives the plain FP32 solve of the
-// mixed path's Krylov basis.  Grid: (tab.nchunks, nrows); arguments as launch_solve.
+// refine64 is set (FP64-accurate result).  refine64 = 0 is the complex64 solve of the mixed
+// path's Krylov basis: one refinement whose residual is formed with error-free FP32 products
+// and sums, complex64 output.  Grid: (tab.nchunks, nrows); arguments as launch_solve.
 cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
                              int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
                              int check_broken, cudaStream_t s);
@@ -160,20 +176,23 @@ cudaError_t launch_tbmv(int arith, int kd, const void* ud_phys, int nl, int nr, 
                         void* out, int out_prec, cudaStream_t s);
 cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsigned* counter, Ctrl* ctrl,
                         cudaStream_t s);
-cudaError_t launch_cgs_dot(int prec, const void* V, long n, int nv, const void* w, double* partials,
-                           unsigned* counter, Ctrl* ctrl, int mode, int want_norm, cudaStream_t s);
+// v0 (complex64 basis only, may be null): FP64 copy of the first basis vector, used in
+// place of V row 0 by the dot, the update and the combination.
+cudaError_t launch_cgs_dot(int prec, const void* V, const double2* v0, long n, int nv, const void* w,
+                           double* partials, unsigned* counter, Ctrl* ctrl, int mode, int want_norm, cudaStream_t s);
 // Stateless block inner product into a caller buffer (out: 2nv doubles, + ||w||^2 when want_norm).
 size_t block_inner_scratch_doubles(long n, int nvals);
 cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const void* w, int want_norm, double* out,
                                double* partials, unsigned* counter, cudaStream_t s);
-cudaError_t launch_cgs_update(int prec, const void* V, long n, int nv, void* w, double* partials,
+cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, long n, int nv, void* w, double* partials,
                               unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
 cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, cudaStream_t s);
 cudaError_t launch_step_begin(Ctrl* ctrl, double* H, int m, cudaStream_t s);
 // max_cluster: 16 lets one problem's exponential spread over a thread-block cluster; 1 keeps it on
 // one CTA (batches, where other problems fill the GPU).
 cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s);
-cudaError_t launch_combine(int prec, const void* V, long n, const Ctrl* ctrl, void* out, cudaStream_t s);
+cudaError_t launch_combine(int prec, const void* V, const double2* v0, long n, const Ctrl* ctrl, void* out,
+                           cudaStream_t s);
 cudaError_t launch_step_end(Ctrl* ctrl, cudaStream_t s);
 cudaError_t launch_tensor_multiply_ref(int storage, const double2* V, int npairs, const int* pairs, int kb,
                                        double scaling, const double2* src, double2* dst, int nl, int nr,

@@ -167,9 +167,10 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
     const int l = blockIdx.y, i0 = blockIdx.x * TILE, tid = threadIdx.x;
     const int nr = op.nr;
     const double scal = sched ? sched[ctrl->step].scaling : scal_val;
-    T yr[PER], yi[PER];
+    const bool kSplit = sizeof(T) < sizeof(double) && op.slots_lo != nullptr;
+    T yr[PER], yi[PER], zr[PER], zi[PER];
 #pragma unroll
-    for (int e = 0; e < PER; ++e) { yr[e] = 0; yi[e] = 0; }
+    for (int e = 0; e < PER; ++e) { yr[e] = 0; yi[e] = 0; zr[e] = 0; zi[e] = 0; }
     const int t0 = op.row_ptr[l], t1 = op.row_ptr[l + 1];
     for (int t = t0; t < t1; ++t) {
         const size_t sbase = (size_t)op.t_src[t] * nr;
@@ -183,6 +184,40 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
         double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
         if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
         const T Cr = (T)cr, Ci = (T)ci;
+        if constexpr (sizeof(T) < sizeof(double)) {
+            if (kSplit) {
+                // complex64 path: error-free products and compensated sums of the band
+                // (coefficient = hi + lo) and of the term factor, so the result is the FP64
+                // operator applied to the complex64 source, rounded once.  The kinetic band's
+                // large alternating entries make plain FP32 sums lose ~eps32 * sum|a s|.
+                const float* Alo = op.slots_lo + (size_t)op.t_slot[t] * W * nr;
+                const float Crl = (float)(cr - (double)Cr), Cil = (float)(ci - (double)Ci);
+#pragma unroll
+                for (int e = 0; e < PER; ++e) {
+                    const int li = tid + e * THREADS;
+                    const int i = i0 + li;
+                    if (i < nr) {
+                        float srh = 0.f, srl = 0.f, sih = 0.f, sil = 0.f;
+#pragma unroll
+                        for (int d = 0; d < W; ++d) {
+                            const C v = sx[li + d];
+                            const float a = __ldg(A + (size_t)d * nr + i), al = __ldg(Alo + (size_t)d * nr + i);
+                            acc_prod(srh, srl, a, al, v.x);
+                            acc_prod(sih, sil, a, al, v.y);
+                        }
+                        if (Cr != 0.f || Crl != 0.f) {
+                            acc_scaled(yr[e], zr[e], Cr, Crl, srh, srl);
+                            acc_scaled(yi[e], zi[e], Cr, Crl, sih, sil);
+                        }
+                        if (Ci != 0.f || Cil != 0.f) {
+                            acc_scaled(yr[e], zr[e], -Ci, -Cil, sih, sil);
+                            acc_scaled(yi[e], zi[e], Ci, Cil, srh, srl);
+                        }
+                    }
+                }
+                continue;
+            }
+        }
 #pragma unroll
         for (int e = 0; e < PER; ++e) {
             const int li = tid + e * THREADS;
@@ -213,7 +248,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
 #pragma unroll
     for (int e = 0; e < PER; ++e) {
         const int i = i0 + tid + e * THREADS;
-        if (i < nr) y[(size_t)l * nr + i] = mk<T>(yr[e], yi[e]);
+        if (i < nr) y[(size_t)l * nr + i] = mk<T>(yr[e] + zr[e], yi[e] + zi[e]);
     }
 }
 
@@ -361,7 +396,8 @@ cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsig
 constexpr int kDotThreads = 256;
 
 template <typename T>
-__global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict__ V, long n, int nv,
+__global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict__ V,
+                                                         const double2* __restrict__ v0, long n, int nv,
                                                          const cx<T>* __restrict__ w, double* partials,
                                                          unsigned* counter, Ctrl* ctrl, int mode, int want_norm,
                                                          double* hout, int epl) {
@@ -374,6 +410,7 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict
     const int k = blockIdx.y, nchunks = gridDim.x, chunk = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const C* vk = k < nv ? V + (size_t)k * n : w;
+    const bool row64 = v0 != nullptr && k == 0;     // complex64 basis with its first vector in FP64
     const long e0 = (long)chunk * kDotThreads * epl + tid;
     double ar[4] = {0.0, 0.0, 0.0, 0.0}, ai[4] = {0.0, 0.0, 0.0, 0.0};
     int t = 0;
@@ -382,8 +419,11 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict
         for (int q = 0; q < 4; ++q) {
             const long e = e0 + (long)(t + q) * kDotThreads;
             if (e < n) {
-                const C v = vk[e], x = w[e];
-                const double vr = (double)v.x, vi = (double)v.y, xr = (double)x.x, xi = (double)x.y;
+                const C x = w[e];
+                double vr, vi;
+                if (row64) { const double2 v = v0[e]; vr = v.x; vi = v.y; }
+                else { const C v = vk[e]; vr = (double)v.x; vi = (double)v.y; }
+                const double xr = (double)x.x, xi = (double)x.y;
                 ar[q] = fma(vr, xr, ar[q]);
                 ar[q] = fma(vi, xi, ar[q]);
                 ai[q] = fma(vr, xi, ai[q]);
@@ -394,8 +434,11 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict
     for (; t < epl; ++t) {
         const long e = e0 + (long)t * kDotThreads;
         if (e < n) {
-            const C v = vk[e], x = w[e];
-            const double vr = (double)v.x, vi = (double)v.y, xr = (double)x.x, xi = (double)x.y;
+            const C x = w[e];
+            double vr, vi;
+            if (row64) { const double2 v = v0[e]; vr = v.x; vi = v.y; }
+            else { const C v = vk[e]; vr = (double)v.x; vi = (double)v.y; }
+            const double xr = (double)x.x, xi = (double)x.y;
             ar[0] = fma(vr, xr, ar[0]);
             ar[0] = fma(vi, xi, ar[0]);
             ai[0] = fma(vr, xi, ai[0]);
@@ -453,18 +496,18 @@ static void dot_shape(long n, int nvals, int* epl, int* nchunks) {
     *nchunks = (int)((n + (long)kDotThreads * e - 1) / ((long)kDotThreads * e));
 }
 
-cudaError_t launch_cgs_dot(int prec, const void* V, long n, int nv, const void* w, double* partials, unsigned* counter,
-                           Ctrl* ctrl, int mode, int want_norm, cudaStream_t s) {
+cudaError_t launch_cgs_dot(int prec, const void* V, const double2* v0, long n, int nv, const void* w, double* partials,
+                           unsigned* counter, Ctrl* ctrl, int mode, int want_norm, cudaStream_t s) {
     count_launch();
     const int nvals = nv + ((want_norm && mode == 0) ? 1 : 0);
     int epl, nch;
     dot_shape(n, nvals, &epl, &nch);
     dim3 grid(nch, nvals);
     if (prec == 0)
-        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, n, nv, (const double2*)w, partials, counter,
-                                                       ctrl, mode, want_norm, nullptr, epl);
+        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, nullptr, n, nv, (const double2*)w, partials,
+                                                       counter, ctrl, mode, want_norm, nullptr, epl);
     else
-        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, n, nv, (const float2*)w, partials, counter,
+        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, v0, n, nv, (const float2*)w, partials, counter,
                                                       ctrl, mode, want_norm, nullptr, epl);
     return cudaGetLastError();
 }
@@ -483,11 +526,11 @@ cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const vo
     dot_shape(n, nvals, &epl, &nch);
     dim3 grid(nch, nvals);
     if (prec == 0)
-        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, n, nv, (const double2*)w, partials, counter,
-                                                       nullptr, 0, want_norm, out, epl);
+        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, nullptr, n, nv, (const double2*)w, partials,
+                                                       counter, nullptr, 0, want_norm, out, epl);
     else
-        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, n, nv, (const float2*)w, partials, counter,
-                                                      nullptr, 0, want_norm, out, epl);
+        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, nullptr, n, nv, (const float2*)w, partials,
+                                                      counter, nullptr, 0, want_norm, out, epl);
     return cudaGetLastError();
 }
 
@@ -499,22 +542,45 @@ cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const vo
 constexpr int kUpdThreads = 256;
 
 template <typename T>
-__global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restrict__ V, long n, int nv,
+__global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restrict__ V,
+                                                            const double2* __restrict__ v0, long n, int nv,
                                                             cx<T>* __restrict__ w, double* partials,
                                                             unsigned* counter, Ctrl* ctrl, int mode) {
     using C = cx<T>;
     __shared__ C hs[kMaxBasis];
+    __shared__ C hl[kMaxBasis];
     if (ctrl->broken) return;
     const int pass = mode & 1;
     const int dorth = (mode >> 1) & 1;
     if (pass == 1 && !ctrl->ro_go) return;
     const double* h = pass ? ctrl->h3 : ctrl->h;
-    for (int k = threadIdx.x; k < nv; k += blockDim.x) hs[k] = mk<T>((T)h[2 * k], (T)h[2 * k + 1]);
+    // complex64 basis: the coefficients keep their FP32 rounding remainders (hl), so the
+    // vector subtracted is V h with the FP64 h of the Hessenberg matrix
+    constexpr bool kSplit = sizeof(T) < sizeof(double);
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+        const T a = (T)h[2 * k], b = (T)h[2 * k + 1];
+        hs[k] = mk<T>(a, b);
+        hl[k] = mk<T>((T)(h[2 * k] - (double)a), (T)(h[2 * k + 1] - (double)b));
+    }
     __syncthreads();
     double acc[1] = {0.0};
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         T sr[4] = {0, 0, 0, 0}, si[4] = {0, 0, 0, 0};
+        T cr = 0, ci = 0;                          // remainder sums (complex64 basis only)
         int k = 0;
+        if (v0) {                                    // first vector kept in FP64: hi + lo parts
+            const double2 a = v0[i];
+            const C hk = hs[0], hlk = hl[0];
+            const T ax = (T)a.x, ay = (T)a.y;
+            const T bx = (T)(a.x - (double)ax), by = (T)(a.y - (double)ay);
+            sr[0] = fma(ax, hk.x, sr[0]);
+            sr[0] = fma(-ay, hk.y, sr[0]);
+            si[0] = fma(ax, hk.y, si[0]);
+            si[0] = fma(ay, hk.x, si[0]);
+            cr = fma(bx, hk.x, cr); cr = fma(-by, hk.y, cr); cr = fma(ax, hlk.x, cr); cr = fma(-ay, hlk.y, cr);
+            ci = fma(bx, hk.y, ci); ci = fma(by, hk.x, ci); ci = fma(ax, hlk.y, ci); ci = fma(ay, hlk.x, ci);
+            k = 1;
+        }
         for (; k + 3 < nv; k += 4) {
             C v[4];
 #pragma unroll
@@ -526,19 +592,33 @@ __global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restr
                 sr[q] = fma(-v[q].y, hk.y, sr[q]);
                 si[q] = fma(v[q].x, hk.y, si[q]);
                 si[q] = fma(v[q].y, hk.x, si[q]);
+                if (kSplit) {
+                    const C hlk = hl[k + q];
+                    cr = fma(v[q].x, hlk.x, cr);
+                    cr = fma(-v[q].y, hlk.y, cr);
+                    ci = fma(v[q].x, hlk.y, ci);
+                    ci = fma(v[q].y, hlk.x, ci);
+                }
             }
         }
         for (; k < nv; ++k) {
-            const C v0 = V[(size_t)k * n + i];
+            const C vk = V[(size_t)k * n + i];
             const C hk = hs[k];
-            sr[0] = fma(v0.x, hk.x, sr[0]);
-            sr[0] = fma(-v0.y, hk.y, sr[0]);
-            si[0] = fma(v0.x, hk.y, si[0]);
-            si[0] = fma(v0.y, hk.x, si[0]);
+            sr[0] = fma(vk.x, hk.x, sr[0]);
+            sr[0] = fma(-vk.y, hk.y, sr[0]);
+            si[0] = fma(vk.x, hk.y, si[0]);
+            si[0] = fma(vk.y, hk.x, si[0]);
+            if (kSplit) {
+                const C hlk = hl[k];
+                cr = fma(vk.x, hlk.x, cr);
+                cr = fma(-vk.y, hlk.y, cr);
+                ci = fma(vk.x, hlk.y, ci);
+                ci = fma(vk.y, hlk.x, ci);
+            }
         }
         C r = w[i];
-        r.x -= (sr[0] + sr[1]) + (sr[2] + sr[3]);
-        r.y -= (si[0] + si[1]) + (si[2] + si[3]);
+        r.x -= ((sr[0] + sr[1]) + (sr[2] + sr[3])) + cr;
+        r.y -= ((si[0] + si[1]) + (si[2] + si[3])) + ci;
         w[i] = r;
         const double re = (double)r.x, im = (double)r.y;
         acc[0] = fma(re, re, acc[0]);
@@ -572,16 +652,16 @@ __global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restr
     }
 }
 
-cudaError_t launch_cgs_update(int prec, const void* V, long n, int nv, void* w, double* partials, unsigned* counter,
-                              Ctrl* ctrl, int mode, cudaStream_t s) {
+cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, long n, int nv, void* w, double* partials,
+                              unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s) {
     count_launch();
     int blocks = (int)((n + kUpdThreads - 1) / kUpdThreads);
     if (blocks > grid_reduce_blocks() * 4) blocks = grid_reduce_blocks() * 4;
     if (prec == 0)
-        k_cgs_update<double><<<blocks, kUpdThreads, 0, s>>>((const double2*)V, n, nv, (double2*)w, partials, counter,
-                                                            ctrl, mode);
+        k_cgs_update<double><<<blocks, kUpdThreads, 0, s>>>((const double2*)V, nullptr, n, nv, (double2*)w, partials,
+                                                            counter, ctrl, mode);
     else
-        k_cgs_update<float><<<blocks, kUpdThreads, 0, s>>>((const float2*)V, n, nv, (float2*)w, partials, counter,
+        k_cgs_update<float><<<blocks, kUpdThreads, 0, s>>>((const float2*)V, v0, n, nv, (float2*)w, partials, counter,
                                                            ctrl, mode);
     return cudaGetLastError();
 }
@@ -1239,7 +1319,8 @@ cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, i
 
 // psi = beta0 * V y  (pamp.h:657-662), FP64 accumulation, complex128 output.
 template <typename T>
-__global__ void k_combine(const cx<T>* __restrict__ V, long n, const Ctrl* __restrict__ ctrl, double2* __restrict__ out) {
+__global__ void k_combine(const cx<T>* __restrict__ V, const double2* __restrict__ v0, long n,
+                          const Ctrl* __restrict__ ctrl, double2* __restrict__ out) {
     __shared__ double2 ys[kMaxBasis];
     const int nb = ctrl->nbasis;
     for (int k = threadIdx.x; k < nb; k += blockDim.x) ys[k] = make_double2(ctrl->y[2 * k], ctrl->y[2 * k + 1]);
@@ -1248,8 +1329,9 @@ __global__ void k_combine(const cx<T>* __restrict__ V, long n, const Ctrl* __res
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         double sr = 0.0, si = 0.0;
         for (int k = 0; k < nb; ++k) {
-            const cx<T> v = V[(size_t)k * n + i];
-            const double vr = (double)v.x, vi = (double)v.y;
+            double vr, vi;
+            if (v0 && k == 0) { const double2 a = v0[i]; vr = a.x; vi = a.y; }
+            else { const cx<T> v = V[(size_t)k * n + i]; vr = (double)v.x; vi = (double)v.y; }
             sr = fma(vr, ys[k].x, sr);
             sr = fma(-vi, ys[k].y, sr);
             si = fma(vr, ys[k].y, si);
@@ -1259,12 +1341,13 @@ __global__ void k_combine(const cx<T>* __restrict__ V, long n, const Ctrl* __res
     }
 }
 
-cudaError_t launch_combine(int prec, const void* V, long n, const Ctrl* ctrl, void* out, cudaStream_t s) {
+cudaError_t launch_combine(int prec, const void* V, const double2* v0, long n, const Ctrl* ctrl, void* out,
+                           cudaStream_t s) {
     count_launch();
     int blocks = (int)((n + 255) / 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
-    if (prec == 0) k_combine<double><<<blocks, 256, 0, s>>>((const double2*)V, n, ctrl, (double2*)out);
-    else k_combine<float><<<blocks, 256, 0, s>>>((const float2*)V, n, ctrl, (double2*)out);
+    if (prec == 0) k_combine<double><<<blocks, 256, 0, s>>>((const double2*)V, nullptr, n, ctrl, (double2*)out);
+    else k_combine<float><<<blocks, 256, 0, s>>>((const float2*)V, v0, n, ctrl, (double2*)out);
     return cudaGetLastError();
 }
 

@@ -480,33 +480,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
     const double sc = scale_mode ? ctrl->inv_beta : 1.0;
     const size_t base = (size_t)l * n;
 
-    if constexpr (!R64) {
-        // plain FP32 solve (complex64 Krylov basis): x = M b
-        for (int q = tid; q < R0 + w; q += kInvThreads) {
-            float2 v = make_float2(0.f, 0.f);
-            if (q < RB) {
-                const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-                const TI t = in[base + p];
-                double2 b = make_double2((double)t.x, (double)t.y);
-                if (scale_mode) { b.x *= sc; b.y *= sc; }
-                if (vstore && q < cl) vstore[base + p] = conv<TV>(b);
-                v = make_float2((float)b.x, (float)b.y);
-            }
-            r32[q] = v;
-        }
-        bool ok = true;
-        if (STAGE) ok = mbar_wait0(&s_bar);
-        if (!__syncthreads_and(ok)) {
-            if (tid == 0) ctrl->wait_timeout = 1;
-            if (STAGE) mbar_wait0(&s_bar);             // let copies in flight land before exit
-            return;
-        }
-        for (int q = tid; q < cl; q += kInvThreads) {
-            const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-            out[base + p] = conv<TO>(inv_apply<STAGE>(mbase + q, mstride, r32, q, w));
-        }
-        return;
-    } else {
+    {
         for (int q = tid; q < RB; q += kInvThreads) {
             const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
             const TI t = in[base + p];
@@ -586,6 +560,154 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
     }
 }
 
+// Complex64 solve of the mixed path's Krylov basis (one CTA per chunk of a row):
+//   x0 = M b_hi                       FP32
+//   r  = b - U~ x0                    FP32 pairs: U~ = uh + ul, b = bh + bl (bl = 0 for a
+//                                     complex64 operand), error-free products and sums
+//   x  = x0 + M r                     FP32, rounded once
+// The refinement makes the operator seen by the basis U^-1 to ~1e-13 (the FP32 band of
+// M alone perturbs it by ~1e-7, which shifts high eigenvalues systematically).  A
+// double2 operand (the FP64 first vector) is used as hi + lo, a complex64 operand as
+// stored, so the solve acts on exactly the vector kept in the basis.
+template <int KD, bool STAGE, typename TI, typename TV>
+__global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const TI* __restrict__ in,
+                                                             float2* __restrict__ out, TV* __restrict__ vstore,
+                                                             Ctrl* __restrict__ ctrl, int dir, int scale_mode,
+                                                             int check_broken) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long s_bar;
+    if (check_broken && ctrl->broken) return;
+    const int n = tab.n, w = tab.w;
+    const int l = blockIdx.y, tid = threadIdx.x;
+    const int q0 = blockIdx.x * tab.chunk;
+    int cl, R0, RB;
+    inv_region(n, q0, tab.chunk, 1, w, KD, &cl, &R0, &RB);
+    const int R0p = (R0 + 3) & ~3;
+    unsigned char* sp = smem_raw;                  // bulk-copy destinations first (16-byte aligned)
+    float* Ms = reinterpret_cast<float*>(sp);
+    float* Uh = Ms + (size_t)(w + 1) * R0p;
+    float* Ul = Uh + (size_t)(KD + 1) * R0p;
+    if (STAGE) sp += (size_t)(w + 1) * R0p * 4 + (size_t)2 * (KD + 1) * R0p * 4;
+    float2* bh = reinterpret_cast<float2*>(sp);
+    float2* bl = bh + RB;
+    float2* x0 = bl + RB;
+    float2* r32 = x0 + R0;
+
+    const float* Mg = tab.m + q0;
+    const float* Uhg = tab.uh + q0;
+    const float* Ulg = tab.ul + q0;
+    if (STAGE) {
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&s_bar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned row = (unsigned)R0p * 4;
+            const unsigned bytes = (unsigned)(w + 1 + 2 * (KD + 1)) * row;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         :: "r"(smem_u32(&s_bar)), "r"(bytes) : "memory");
+            for (int j = 0; j <= w; ++j) bulk_g2s(Ms + (size_t)j * R0p, Mg + (size_t)j * tab.npad, row, &s_bar);
+            for (int d = 0; d <= KD; ++d) {
+                bulk_g2s(Uh + (size_t)d * R0p, Uhg + (size_t)d * tab.npad, row, &s_bar);
+                bulk_g2s(Ul + (size_t)d * R0p, Ulg + (size_t)d * tab.npad, row, &s_bar);
+            }
+        }
+    }
+    const float* mbase = STAGE ? Ms : Mg;
+    const size_t mstride = STAGE ? (size_t)R0p : (size_t)tab.npad;
+    const float* uhb = STAGE ? Uh : Uhg;
+    const float* ulb = STAGE ? Ul : Ulg;
+    const size_t ustride = STAGE ? (size_t)R0p : (size_t)tab.npad;
+    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
+    const size_t base = (size_t)l * n;
+    constexpr bool kWide = sizeof(TI) == sizeof(double2);
+    for (int q = tid; q < R0 + w; q += kInvThreads) {
+        float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
+        if (q < RB) {
+            const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+            const TI t = in[base + p];
+            double2 b = make_double2((double)t.x, (double)t.y);
+            if (scale_mode) { b.x *= sc; b.y *= sc; }
+            hi = make_float2((float)b.x, (float)b.y);
+            if (kWide) lo = make_float2((float)(b.x - (double)hi.x), (float)(b.y - (double)hi.y));
+            if (vstore && q < cl) {
+                if (sizeof(TV) == sizeof(double2)) vstore[base + p] = conv<TV>(b);
+                else vstore[base + p] = conv<TV>(hi);
+            }
+            bh[q] = hi;
+            bl[q] = lo;
+        }
+        r32[q] = hi;
+    }
+    bool ok = true;
+    if (STAGE) ok = mbar_wait0(&s_bar);
+    if (!__syncthreads_and(ok)) {
+        if (tid == 0) ctrl->wait_timeout = 1;
+        if (STAGE) mbar_wait0(&s_bar);             // let copies in flight land before exit
+        return;
+    }
+    for (int q = tid; q < R0; q += kInvThreads) x0[q] = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
+    __syncthreads();
+    const int Rr = min(n - q0, cl + w);
+    for (int q = tid; q < cl + w; q += kInvThreads) {
+        float2 r = make_float2(0.f, 0.f);
+        if (q < Rr) {
+            float hr = 0.f, lr = 0.f, hi_ = 0.f, li = 0.f;
+#pragma unroll
+            for (int d = 0; d <= KD; ++d) {
+                if (q + d < n - q0) {
+                    const float uh = uhb[(size_t)d * ustride + q], ul = ulb[(size_t)d * ustride + q];
+                    const float2 xv = x0[q + d];
+                    acc_prod(hr, lr, uh, ul, xv.x);
+                    acc_prod(hi_, li, uh, ul, xv.y);
+                }
+            }
+            const float2 b_h = bh[q], b_l = bl[q];
+            float s, e;
+            two_sum(b_h.x, -hr, s, e);
+            r.x = __fadd_rn(s, __fadd_rn(e, __fsub_rn(b_l.x, lr)));
+            two_sum(b_h.y, -hi_, s, e);
+            r.y = __fadd_rn(s, __fadd_rn(e, __fsub_rn(b_l.y, li)));
+        }
+        r32[q] = r;
+    }
+    __syncthreads();
+    for (int q = tid; q < cl; q += kInvThreads) {
+        const float2 d = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
+        const float2 x = x0[q];
+        const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+        out[base + p] = make_float2(__fadd_rn(x.x, d.x), __fadd_rn(x.y, d.y));
+    }
+}
+
+template <int KD, bool STAGE>
+static cudaError_t solve_mixed_launch(const InvTab& tab, int nrows, const void* in, int in_prec, void* out,
+                                      int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
+                                      int check_broken, cudaStream_t s) {
+    if (out_prec != 1) return cudaErrorInvalidValue;
+    size_t smem = 0;
+    for (int c = 0; c < tab.nchunks; ++c)
+        smem = std::max(smem, inv_smem_bytes_mixed(tab.n, c * tab.chunk, tab.chunk, tab.w, KD, STAGE));
+    dim3 grid(tab.nchunks, nrows), block(kInvThreads);
+#define GB_MIX_CASE(TI_, TV_)                                                                                    \
+    {                                                                                                            \
+        auto kern = k_solve_mixed<KD, STAGE, TI_, TV_>;                                                          \
+        if (smem > 48 * 1024) {                                                                                  \
+            cudaError_t ea = allow_max_smem(kern);                                                               \
+            if (ea != cudaSuccess) return ea;                                                                    \
+        }                                                                                                        \
+        kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (float2*)out, (TV_*)vstore, ctrl, dir, scale_mode,   \
+                                       check_broken);                                                            \
+        return cudaGetLastError();                                                                               \
+    }
+    // in: the FP64 first vector (with its FP64 copy stored) or a complex64 vector
+    if (in_prec == 0 && v_prec == 0) GB_MIX_CASE(double2, double2)
+    if (in_prec == 1) GB_MIX_CASE(float2, float2)
+#undef GB_MIX_CASE
+    return cudaErrorInvalidValue;
+}
+
 template <int KD, bool R64, bool STAGE>
 static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in, int in_prec, void* out,
                                     int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir,
@@ -606,23 +728,14 @@ static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in
                                        check_broken);                                                            \
         return cudaGetLastError();                                                                               \
     }
-    // combinations the runtime uses: refined solves store double2 (or nothing), the plain
-    // FP32 solve of the mixed basis writes and stores complex64
+    // combinations the runtime uses: refined solves store double2 (or nothing)
     const int key = in_prec * 4 + out_prec * 2 + v_prec;
-    if constexpr (R64) {
-        switch (key) {
-            case 0: GB_INV_CASE(double2, double2, double2)
-            case 2: GB_INV_CASE(double2, float2, double2)
-            case 4: GB_INV_CASE(float2, double2, double2)
-            case 6: GB_INV_CASE(float2, float2, double2)
-            default: return cudaErrorInvalidValue;
-        }
-    } else {
-        switch (key) {
-            case 3: GB_INV_CASE(double2, float2, float2)
-            case 7: GB_INV_CASE(float2, float2, float2)
-            default: return cudaErrorInvalidValue;
-        }
+    switch (key) {
+        case 0: GB_INV_CASE(double2, double2, double2)
+        case 2: GB_INV_CASE(double2, float2, double2)
+        case 4: GB_INV_CASE(float2, double2, double2)
+        case 6: GB_INV_CASE(float2, float2, double2)
+        default: return cudaErrorInvalidValue;
     }
 #undef GB_INV_CASE
 }
@@ -639,10 +752,10 @@ static cudaError_t solve_inv_kd(const InvTab& tab, int nrows, int refine64, cons
                                                  scale_mode, check_broken, s);
     }
     if (tab.stage)
-        return solve_inv_launch<KD, false, true>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
-                                                 scale_mode, check_broken, s);
-    return solve_inv_launch<KD, false, false>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
-                                              scale_mode, check_broken, s);
+        return solve_mixed_launch<KD, true>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
+                                            scale_mode, check_broken, s);
+    return solve_mixed_launch<KD, false>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
+                                         scale_mode, check_broken, s);
 }
 
 cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,

@@ -1,0 +1,101 @@
+"""Final-state observables of the hydrogen examples: bound-state populations and
+ionisation probability.
+
+The field-free bound states are the eigenvectors with E < 0 of the static
+(time-independent, angular-diagonal) TensorPotentials in the B-spline overlap metric,
+one generalized eigenproblem H0_l c = E S c per angular row l; the population of state b
+is |<phi_b|S|psi>|^2 and the ionisation probability 1 - sum_b |<phi_b|S|psi>|^2 (for a
+normalised psi).  This follows the analysis of the reference's hydrogen example
+(examples/tensor/helium_stabilization_sae/analysis.py:92-160, 344-375), restated.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .tensorpotential import bandnh_to_dense
+
+
+def _dense_from_diagonals(D, kd, n):
+    S = np.zeros((n, n))
+    for d in range(-kd, kd + 1):
+        i = np.arange(max(0, -d), min(n, n - d))
+        S[i, i + d] = D[kd + d, i]
+    return S
+
+
+def bound_states(nl, nr, kb, S, static_rows, emax=0.0, lmax_states=None):
+    """Bound eigenstates of the angular-diagonal static operator.
+
+    S: dense radial overlap (nr, nr); static_rows[l]: BandNH data of row l (complex, real-valued).
+    Returns (states (nb, nl*nr) complex, S-normalised; energies (nb,); l of each state (nb,))."""
+    import scipy.linalg as sl
+    states, energies, ls = [], [], []
+    last = nl if lmax_states is None else min(nl, lmax_states + 1)
+    for l in range(last):
+        H = bandnh_to_dense(np.asarray(static_rows[l]), nr, kb).real
+        H = 0.5 * (H + H.T)
+        e, v = sl.eigh(H, S)
+        for j in np.where(e < emax)[0]:
+            phi = np.zeros((nl, nr), dtype=np.complex128)
+            phi[l] = v[:, j] / math.sqrt(v[:, j] @ S @ v[:, j])
+            states.append(phi.ravel())
+            energies.append(e[j])
+            ls.append(l)
+    return np.array(states), np.array(energies), np.array(ls)
+
+
+def problem_bound_states(problem, emax=0.0, lmax_states=None):
+    """bound_states() of a pyprop_gb300.Problem (its consolidated static Diag potentials)."""
+    repr_ = problem.psi.GetRepresentation()
+    nl, nr = repr_.GetFullShape()
+    rad = repr_.radial
+    S = _dense_from_diagonals(rad.overlap_diagonals(), rad.kd, nr)
+    static = None
+    kb = rad.kd
+    for p in problem.Propagator.BasePropagator.PotentialList:
+        if p.IsTimeDependent:
+            continue
+        s0, _ = p.GetStorageIds()
+        kb = p.GeometryList[1].band_count
+        if s0 == "Diag":
+            rows = np.asarray(p.PotentialData)
+        elif s0 == "Ident":
+            rows = np.repeat(np.asarray(p.PotentialData), nl, axis=0)
+        else:
+            raise NotImplementedError("bound states need angular-diagonal static potentials (got %s)" % s0)
+        static = rows if static is None else static + rows
+    return bound_states(nl, nr, kb, S, static, emax, lmax_states)
+
+
+def hydrogen_bound_states(hp, emax=0.0, lmax_states=None):
+    """bound_states() of a batch.HydrogenProblem."""
+    S = _dense_from_diagonals(hp.Sdiag, hp.kd, hp.nr)
+    return bound_states(hp.nl, hp.nr, hp.kb, S, hp.static, emax, lmax_states)
+
+
+def populations(psi, states, S):
+    """|<phi_b|S|psi>|^2 per state; psi (nl, nr) numpy, S dense radial overlap."""
+    psi = np.asarray(psi, dtype=np.complex128)
+    Spsi = (psi @ S.T).ravel()
+    amps = np.conj(states) @ Spsi
+    return np.abs(amps) ** 2
+
+
+def overlap_norm2(psi, S):
+    psi = np.asarray(psi, dtype=np.complex128)
+    return float(np.real(np.sum(np.conj(psi) * (psi @ S.T))))
+
+
+def report(psi, states, S):
+    """Populations per bound state, their sum and the ionisation probability 1 - sum."""
+    pops = populations(psi, states, S)
+    norm = overlap_norm2(psi, S)
+    return {"populations": pops, "bound": float(pops.sum()), "ionisation": float(norm - pops.sum()), "norm": norm}
+
+
+def radial_overlap(problem):
+    """Dense radial overlap matrix of a Problem."""
+    rad = problem.psi.GetRepresentation().radial
+    return _dense_from_diagonals(rad.overlap_diagonals(), rad.kd, rad.count)

@@ -71,4 +71,4 @@ def test_batch_mixed_precision_error_report():
         want, _ = _oracle(p).advance(psi0[i], p.m, p.dt, bp.scalings(i, 5))
         errs.append(rel(bp.psi[i].cpu().numpy().astype(np.complex128), want))
     print("FP32-mixed batch, 5 steps, relative L2 vs FP64 oracle per problem:", ["%.2e" % e for e in errs])
-    assert max(errs) < 1e-3
+    assert max(errs) < 1e-5

@@ -278,9 +278,9 @@ def test_mixed_precision_error_report():
         pass
     err = rel(prob.psi.GetDataNumpy().astype(np.complex128), g["psi500"])
     print("500-step FP32-mixed relative L2 vs FP64 oracle: %.3e" % err)
-    # complex64 matvec rounding perturbs the Ritz values by ~eps32 * ||H|| (||H|| ~ 1.6e4 for
-    # this random initial state): regression bound for the plain mixed mode
-    assert err < 2e-3
+    # complex64 rounding of the Krylov vectors of this random (high-energy) state: regression
+    # bound; the ground-state case and the observables are in test_gpu_mixed.py
+    assert err < 1e-4
 
 
 @pytest.mark.parametrize("prec,n,nv", [(0, 64000, 11), (0, 1060, 1), (1, 5003, 30), (0, 77, 45)])
