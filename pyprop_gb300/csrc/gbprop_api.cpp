@@ -1049,14 +1049,15 @@ struct gbprop_batch_ctx {
     cudaStream_t stream = nullptr, ustream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_in = nullptr, ev_out = nullptr;
     std::vector<cudaEvent_t> ev_join;
-    cudaGraphExec_t graph = nullptr;                  // one step of every problem
-    cudaGraphExec_t g_enter = nullptr, g_leave = nullptr;   // x = U psi / psi = U^-1 x of every problem
+    // one batch step per graph launch; each problem is one branch whose kernels are, per
+    // shape: [0] enter + step + leave (one-step calls), [1] enter + step (first step),
+    // [2] step (middle steps), [3] step + leave (last step)
+    cudaGraphExec_t g[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long g_launches[4] = {0, 0, 0, 0};
     std::vector<void*> graph_psi;
-    long long graph_launches = 0, enter_launches = 0, leave_launches = 0;
     ~gbprop_batch_ctx() {
-        if (graph) cudaGraphExecDestroy(graph);
-        if (g_enter) cudaGraphExecDestroy(g_enter);
-        if (g_leave) cudaGraphExecDestroy(g_leave);
+        for (cudaGraphExec_t x : g)
+            if (x) cudaGraphExecDestroy(x);
         for (cudaEvent_t e : ev_join) cudaEventDestroy(e);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_in) cudaEventDestroy(ev_in);
@@ -1068,7 +1069,7 @@ struct gbprop_batch_ctx {
 namespace {
 
 // Capture one parallel branch per problem (forked from and joined into the batch stream).
-// what: 0 = one step, 1 = enter (x = U psi), 2 = leave (psi = U^-1 x).
+// what: bit 0 = enter (x = U psi), bit 1 = one step, bit 2 = leave (psi = U^-1 x).
 gbprop_status batch_capture(gbprop_batch b, void* const* psi, int what, cudaGraphExec_t* out, long long* launches) {
     if (*out) {
         cudaGraphExecDestroy(*out);
@@ -1083,8 +1084,9 @@ gbprop_status batch_capture(gbprop_batch b, void* const* psi, int what, cudaGrap
         gbprop_ctx* h = b->hs[p];
         e = cudaStreamWaitEvent(h->stream, b->ev_fork, 0);
         if (e != cudaSuccess) break;
-        st = what == 0 ? enqueue_step(h) : what == 1 ? enqueue_enter(h, psi[p], h->stream)
-                                                     : enqueue_leave(h, psi[p], h->stream);
+        if (what & 1) st = enqueue_enter(h, psi[p], h->stream);
+        if (!st && (what & 2)) st = enqueue_step(h);
+        if (!st && (what & 4)) st = enqueue_leave(h, psi[p], h->stream);
         if (st) break;
         e = cudaEventRecord(b->ev_join[p], h->stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_join[p], 0);
@@ -1161,22 +1163,24 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
         if (!psi[p]) return fail(GBPROP_EINVAL, "null wavefunction in batch");
     GB_CUDA(cudaEventRecord(b->ev_in, b->ustream));
     GB_CUDA(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
-    bool new_psi = b->graph_psi.size() != P || !b->g_enter || !b->g_leave;
+    static const int kShape[4] = {1 | 2 | 4, 1 | 2, 2, 2 | 4};
+    bool new_psi = b->graph_psi.size() != P;
     for (size_t p = 0; p < P && !new_psi; ++p)
         if (b->graph_psi[p] != psi[p]) new_psi = true;
     if (new_psi) {
-        if (gbprop_status st = batch_capture(b, psi, 1, &b->g_enter, &b->enter_launches)) return st;
-        if (gbprop_status st = batch_capture(b, psi, 2, &b->g_leave, &b->leave_launches)) return st;
+        for (int k : {0, 1, 3})
+            if (b->g[k]) {
+                cudaGraphExecDestroy(b->g[k]);
+                b->g[k] = nullptr;
+            }
         b->graph_psi.assign(psi, psi + P);
     }
-    GB_CUDA(cudaGraphLaunch(b->g_enter, b->stream));
-    count_launch((int)b->enter_launches);
     int done = 0;
     while (done < nsteps) {
         int cap = 1 << 30;
         for (gbprop_handle h : b->hs) cap = std::min(cap, std::max(h->sched_cap, 1024));
         const int chunk = std::min(nsteps - done, cap);
-        bool recapture = !b->graph;
+        bool recapture = false;
         for (size_t p = 0; p < P; ++p) {
             gbprop_ctx* h = b->hs[p];
             const int old_cap = h->sched_cap;
@@ -1190,15 +1194,23 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
             GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), b->stream));
         }
         if (recapture)
-            if (gbprop_status st = batch_capture(b, psi, 0, &b->graph, &b->graph_launches)) return st;
+            for (int k = 0; k < 4; ++k)
+                if (b->g[k]) {
+                    cudaGraphExecDestroy(b->g[k]);
+                    b->g[k] = nullptr;
+                }
         for (int k = 0; k < chunk; ++k) {
-            GB_CUDA(cudaGraphLaunch(b->graph, b->stream));
-            count_launch((int)b->graph_launches);
+            const int step = done + k;
+            const bool first = step == 0, last = step == nsteps - 1;
+            const int shape = first && last ? 0 : first ? 1 : last ? 3 : 2;
+            if (!b->g[shape])
+                if (gbprop_status st = batch_capture(b, psi, kShape[shape], &b->g[shape], &b->g_launches[shape]))
+                    return st;
+            GB_CUDA(cudaGraphLaunch(b->g[shape], b->stream));
+            count_launch((int)b->g_launches[shape]);
         }
         done += chunk;
     }
-    GB_CUDA(cudaGraphLaunch(b->g_leave, b->stream));
-    count_launch((int)b->leave_launches);
     GB_CUDA(cudaEventRecord(b->ev_out, b->stream));
     GB_CUDA(cudaStreamWaitEvent(b->ustream, b->ev_out, 0));
     return GBPROP_OK;

@@ -197,14 +197,26 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
                     const int li = tid + e * THREADS;
                     const int i = i0 + li;
                     if (i < nr) {
+                        // even and odd diagonals in separate compensated chains, merged exactly
                         float srh = 0.f, srl = 0.f, sih = 0.f, sil = 0.f;
+                        float orh = 0.f, orl = 0.f, oih = 0.f, oil = 0.f;
 #pragma unroll
                         for (int d = 0; d < W; ++d) {
                             const C v = sx[li + d];
                             const float a = __ldg(A + (size_t)d * nr + i), al = __ldg(Alo + (size_t)d * nr + i);
-                            acc_prod(srh, srl, a, al, v.x);
-                            acc_prod(sih, sil, a, al, v.y);
+                            if (d & 1) {
+                                acc_prod(orh, orl, a, al, v.x);
+                                acc_prod(oih, oil, a, al, v.y);
+                            } else {
+                                acc_prod(srh, srl, a, al, v.x);
+                                acc_prod(sih, sil, a, al, v.y);
+                            }
                         }
+                        float t;
+                        two_sum(srh, orh, srh, t);
+                        srl = __fadd_rn(__fadd_rn(srl, orl), t);
+                        two_sum(sih, oih, sih, t);
+                        sil = __fadd_rn(__fadd_rn(sil, oil), t);
                         if (Cr != 0.f || Crl != 0.f) {
                             acc_scaled(yr[e], zr[e], Cr, Crl, srh, srl);
                             acc_scaled(yi[e], zi[e], Cr, Crl, sih, sil);
@@ -414,6 +426,43 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict
     const long e0 = (long)chunk * kDotThreads * epl + tid;
     double ar[4] = {0.0, 0.0, 0.0, 0.0}, ai[4] = {0.0, 0.0, 0.0, 0.0};
     int t = 0;
+    if constexpr (sizeof(T) < sizeof(double)) {
+        if (!row64) {
+            // complex64 operands: error-free FP32 products and compensated FP32 sums (the
+            // result equals the FP64 dot to ~2^-48); FP64 only for the block reduction
+            float rh0 = 0.f, rl0 = 0.f, ih0 = 0.f, il0 = 0.f, rh1 = 0.f, rl1 = 0.f, ih1 = 0.f, il1 = 0.f;
+            for (; t + 1 < epl; t += 2) {
+                const long ea = e0 + (long)t * kDotThreads, eb = ea + kDotThreads;
+                if (ea < n) {
+                    const C v = vk[ea], x = w[ea];
+                    acc_prod(rh0, rl0, v.x, 0.f, x.x);
+                    acc_prod(rh0, rl0, v.y, 0.f, x.y);
+                    acc_prod(ih0, il0, v.x, 0.f, x.y);
+                    acc_prod(ih0, il0, -v.y, 0.f, x.x);
+                }
+                if (eb < n) {
+                    const C v = vk[eb], x = w[eb];
+                    acc_prod(rh1, rl1, v.x, 0.f, x.x);
+                    acc_prod(rh1, rl1, v.y, 0.f, x.y);
+                    acc_prod(ih1, il1, v.x, 0.f, x.y);
+                    acc_prod(ih1, il1, -v.y, 0.f, x.x);
+                }
+            }
+            for (; t < epl; ++t) {
+                const long ea = e0 + (long)t * kDotThreads;
+                if (ea < n) {
+                    const C v = vk[ea], x = w[ea];
+                    acc_prod(rh0, rl0, v.x, 0.f, x.x);
+                    acc_prod(rh0, rl0, v.y, 0.f, x.y);
+                    acc_prod(ih0, il0, v.x, 0.f, x.y);
+                    acc_prod(ih0, il0, -v.y, 0.f, x.x);
+                }
+            }
+            ar[0] = ((double)rh0 + (double)rl0) + ((double)rh1 + (double)rl1);
+            ai[0] = ((double)ih0 + (double)il0) + ((double)ih1 + (double)il1);
+            t = epl;
+        }
+    }
     for (; t + 3 < epl; t += 4) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -953,9 +1002,9 @@ __global__ void __launch_bounds__(256) k_expm(Ctrl* ctrl, double* Hg, int m, con
 // CTAs of a thread-block cluster.  Each CTA keeps full copies of the matrices in
 // its shared memory; a product's rows are computed by their owner CTA (row % CL)
 // and stored into every CTA's copy through distributed shared memory, followed by
-// a cluster barrier.  The LU factorisation of Q-P runs redundantly in every CTA
+// a cluster barrier.  The FP32 inversion of Q-P runs redundantly in every CTA
 // (identical arithmetic, so identical results); the m right-hand sides of the
-// solve are split over the CTAs by column.  FP64 throughput is ~2 FMA/clk/SM on
+// refined solve are split over the CTAs by column.  FP64 throughput is ~2 FMA/clk/SM on
 // GB300, so spreading the products over CL SMs is what makes this step cheap.
 // ---------------------------------------------------------------------------
 namespace cg = cooperative_groups;
@@ -1012,26 +1061,36 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
     double2* LU = buf[5];
     double2* X = buf[6];
     __shared__ double red[8];
-    __shared__ int piv[kMaxBasis];
     __shared__ int s_p;
     __shared__ int s_info;
     __shared__ double s_c[8];
     const int tid = threadIdx.x;
     const SchedEntry se = sched[ctrl->step];
     const double2 f = make_double2(se.dt_im, -se.dt_re);   // -i * dt (pamp.h:634)
+    // max |a|^2 (no FP64 square roots or divisions on the wide path: they are long
+    // instruction sequences on this part's FP64 unit)
     double mx = 0.0;
     for (int k = tid; k < mm; k += blockDim.x) {
         const double2 a = cmulz(make_double2(Hg[2 * k], Hg[2 * k + 1]), f);
         A[k] = a;
-        mx = fmax(mx, hypot(a.x, a.y));
+        mx = fmax(mx, fma(a.x, a.x, a.y * a.y));
     }
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((tid & 31) == 0) red[tid >> 5] = mx;
     __syncthreads();
     if (tid == 0) {
-        double v = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, red[w]);
-        int sord = v > 0.0 ? (int)ceil(log2(v)) : 0;
+        double v2 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v2 = fmax(v2, red[w]);
+        // s = max(0, ceil(log2 max|a|)) (pamp.h:441-447): from the exponent of max|a|,
+        // exact except when max|a| is a power of two, which frexp resolves
+        int sord = 0;
+        if (!(v2 <= DBL_MAX)) {
+            ctrl->nonfinite = 1;                        // Inf/NaN Hessenberg: no scaling, flag it
+        } else if (v2 > 0.0) {
+            int e;
+            const double fr = frexp(sqrt(v2), &e);      // max|a| = fr * 2^e, fr in [0.5, 1)
+            sord = (fr == 0.5) ? e - 1 : e;
+        }
         if (sord < 0) sord = 0;
         s_p = sord;
         s_info = 0;
@@ -1041,8 +1100,8 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
     }
     __syncthreads();
     const int sorder = s_p;
-    const double sc = pow(2.0, (double)sorder);
-    for (int k = tid; k < mm; k += blockDim.x) { A[k].x /= sc; A[k].y /= sc; }
+    const double isc = ldexp(1.0, -sorder);            // exact power of two
+    for (int k = tid; k < mm; k += blockDim.x) { A[k].x *= isc; A[k].y *= isc; }
     // every CTA scaled its own copy of A: barrier before anyone writes remotely
     cl.sync();
     if (rank == 0)
@@ -1075,22 +1134,31 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
     cl_matmul<CL>(cl, rank, m, P, A, T);                   // P = P A
     { double2* t = P; P = T; T = t; }
     // X = (Q - P)^-1 P (pamp.h:541-556).  D = Q - P is the Pade denominator, well
-    // conditioned after scaling; it is inverted approximately in FP32 (LU with
-    // partial pivoting, then the m unit right-hand sides), and X is refined twice
+    // conditioned after scaling; it is inverted approximately in FP32 (Gauss-Jordan
+    // with partial pivoting), and X is refined twice
     // with FP64 residuals R = P - D X.  Each refinement squares the FP32 error
     // (~1e-6), so X is FP64-accurate; only the FP64 residual products are
     // throughput-heavy and they are split over the cluster by column.
     for (int k = tid; k < mm; k += blockDim.x) LU[k] = make_double2(Q[k].x - P[k].x, Q[k].y - P[k].y);   // D (FP64)
-    float2* F = reinterpret_cast<float2*>(X);            // FP32 LU of D      (m*m float2)
-    float2* Z = F + mm;                                  // FP32 inverse of D (m*m float2)
-    for (int k = tid; k < mm; k += blockDim.x) F[k] = make_float2((float)LU[k].x, (float)LU[k].y);
+    __syncthreads();                                      // D is read below with another mapping
+    // Z = D^-1 in FP32 by Gauss-Jordan elimination with partial pivoting on |re|+|im|
+    // (all threads update the m x 2m block [D | I] at every pivot step)
+    float2* F = reinterpret_cast<float2*>(X);            // [D | I] rows of 2m float2 (m*2m float2)
+    const int w2 = 2 * m;
+    const float2* Z = F + m;                              // the inverse ends in the right half:
+                                                          // Z(r, k) = Z[r * w2 + k]
+    for (int k = tid; k < m * w2; k += blockDim.x) {
+        const int r = k / w2, c = k - r * w2;
+        F[k] = c < m ? make_float2((float)LU[r * m + c].x, (float)LU[r * m + c].y)
+                     : make_float2(c - m == r ? 1.f : 0.f, 0.f);
+    }
     __syncthreads();
     for (int k = 0; k < m; ++k) {
         if (tid < 32) {
             float best = -1.f;
             int bi = k;
             for (int r = k + tid; r < m; r += 32) {
-                const float v = fabsf(F[r * m + k].x) + fabsf(F[r * m + k].y);
+                const float v = fabsf(F[r * w2 + k].x) + fabsf(F[r * w2 + k].y);
                 if (v > best) { best = v; bi = r; }
             }
             for (int o = 16; o > 0; o >>= 1) {
@@ -1099,38 +1167,42 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
             if (tid == 0) {
-                piv[k] = bi;
                 if (best == 0.f && !s_info) s_info = k + 1;
                 s_p = (best == 0.f) ? -1 : bi;
             }
         }
         __syncthreads();
         const int p = s_p;
-        if (p >= 0) {
-            if (p != k)
-                for (int c = tid; c < m; c += blockDim.x) {
-                    const float2 t = F[k * m + c];
-                    F[k * m + c] = F[p * m + c];
-                    F[p * m + c] = t;
-                }
-            __syncthreads();
-            const float2 d = F[k * m + k];
-            const float den = d.x * d.x + d.y * d.y;
-            const float2 inv = make_float2(d.x / den, -d.y / den);
-            for (int r = k + 1 + tid; r < m; r += blockDim.x) {
-                const float2 a = F[r * m + k];
-                F[r * m + k] = make_float2(a.x * inv.x - a.y * inv.y, a.x * inv.y + a.y * inv.x);
+        if (p < 0) break;                                  // singular (uniform: s_p is shared)
+        // swap rows k and p, then scale row k by 1/pivot (one thread per column)
+        for (int c = tid; c < w2; c += blockDim.x) {
+            float2 a = F[k * w2 + c];
+            if (p != k) {
+                const float2 b = F[p * w2 + c];
+                F[p * w2 + c] = a;
+                a = b;
             }
-            __syncthreads();
-            const int rem = m - k - 1;
-            for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
-                const int r = k + 1 + idx / rem, c = k + 1 + idx % rem;
-                const float2 fr = F[r * m + k], u = F[k * m + c];
-                float2 q = F[r * m + c];
-                q.x -= fr.x * u.x - fr.y * u.y;
-                q.y -= fr.x * u.y + fr.y * u.x;
-                F[r * m + c] = q;
-            }
+            F[k * w2 + c] = a;
+        }
+        __syncthreads();
+        const float2 d = F[k * w2 + k];
+        const float den = d.x * d.x + d.y * d.y;
+        const float2 inv = make_float2(d.x / den, -d.y / den);
+        __syncthreads();
+        for (int c = tid; c < w2; c += blockDim.x) {
+            const float2 a = F[k * w2 + c];
+            F[k * w2 + c] = make_float2(a.x * inv.x - a.y * inv.y, a.x * inv.y + a.y * inv.x);
+        }
+        __syncthreads();
+        // eliminate column k from every other row
+        for (int idx = tid; idx < m * w2; idx += blockDim.x) {
+            const int r = idx / w2, c = idx - r * w2;
+            if (r == k || c <= k) continue;
+            const float2 fr = F[r * w2 + k], u = F[k * w2 + c];
+            float2 q = F[r * w2 + c];
+            q.x -= fr.x * u.x - fr.y * u.y;
+            q.y -= fr.x * u.y + fr.y * u.x;
+            F[r * w2 + c] = q;
         }
         __syncthreads();
     }
@@ -1138,56 +1210,39 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
     if (info) {
         if (rank == 0 && tid == 0) ctrl->lu_info = info;
     } else {
-        // Z = D^-1 in FP32: thread c solves L U z = P_perm e_c
-        for (int c = tid; c < m; c += blockDim.x) {
-            float2 z[kMaxBasis];
-            for (int r = 0; r < m; ++r) z[r] = make_float2(0.f, 0.f);
-            z[c] = make_float2(1.f, 0.f);
-            for (int k = 0; k < m; ++k) {          // row interchanges in order
-                const int pk = piv[k];
-                if (pk != k) { const float2 t = z[k]; z[k] = z[pk]; z[pk] = t; }
-            }
-            for (int r = 0; r < m; ++r) {
-                float2 a = z[r];
-                for (int k = 0; k < r; ++k) {
-                    const float2 l = F[r * m + k];
-                    a.x -= l.x * z[k].x - l.y * z[k].y;
-                    a.y -= l.x * z[k].y + l.y * z[k].x;
-                }
-                z[r] = a;
-            }
-            for (int r = m - 1; r >= 0; --r) {
-                float2 a = z[r];
-                for (int k = r + 1; k < m; ++k) {
-                    const float2 u = F[r * m + k];
-                    a.x -= u.x * z[k].x - u.y * z[k].y;
-                    a.y -= u.x * z[k].y + u.y * z[k].x;
-                }
-                const float2 d = F[r * m + r];
-                const float den = d.x * d.x + d.y * d.y;
-                z[r] = make_float2((a.x * d.x + a.y * d.y) / den, (a.y * d.x - a.x * d.y) / den);
-            }
-            for (int r = 0; r < m; ++r) Z[r * m + c] = z[r];
-        }
-        __syncthreads();
         // this CTA's columns c = rank + j*CL of X (FP64, kept in T), residual R in Q's buffer
         const int ncol = (m - rank + CL - 1) / CL;
         double2* Xc = T;
         double2* R = Q;
+        // FP32 copy of the residual: A is free after P = P A and, unlike A2 (the target of
+        // the E broadcast) and T (matmul target), never written by another CTA
+        float2* R32 = reinterpret_cast<float2*>(A);
         for (int it = 0; it < 3; ++it) {
-            // R = P - D X  (it == 0: R = P, X = 0)
-            for (int idx = tid; idx < ncol * m; idx += blockDim.x) {
-                const int c = rank + (idx / m) * CL, r = idx % m;
-                double rr = P[r * m + c].x, ri = P[r * m + c].y;
-                if (it > 0)
-                    for (int k = 0; k < m; ++k) {
+            // R = P - D X  (it == 0: R = P, X = 0); four threads per entry split the k sum
+            // (independent FP64 chains), combined by shuffles within aligned lane quads
+            for (int base = 0; base < ncol * m * 4; base += blockDim.x) {
+                const int idx = base + tid, ks = idx & 3, o = idx >> 2;
+                const bool act = o < ncol * m;
+                const int c = act ? rank + (o / m) * CL : 0, r = act ? o % m : 0;
+                double ra = 0.0, rb = 0.0, ia = 0.0, ib = 0.0;
+                if (act && it > 0)
+                    for (int k = ks; k < m; k += 4) {
                         const double2 d = LU[r * m + k], x = Xc[k * m + c];
-                        rr = fma(-d.x, x.x, rr);
-                        rr = fma(d.y, x.y, rr);
-                        ri = fma(-d.x, x.y, ri);
-                        ri = fma(-d.y, x.x, ri);
+                        ra = fma(-d.x, x.x, ra);
+                        rb = fma(d.y, x.y, rb);
+                        ia = fma(-d.x, x.y, ia);
+                        ib = fma(-d.y, x.x, ib);
                     }
-                R[r * m + c] = make_double2(rr, ri);
+                double rr = ra + rb, ri = ia + ib;
+                rr += __shfl_xor_sync(0xffffffffu, rr, 1);
+                ri += __shfl_xor_sync(0xffffffffu, ri, 1);
+                rr += __shfl_xor_sync(0xffffffffu, rr, 2);
+                ri += __shfl_xor_sync(0xffffffffu, ri, 2);
+                if (act && ks == 0) {
+                    const double2 v = make_double2(P[r * m + c].x + rr, P[r * m + c].y + ri);
+                    R[r * m + c] = v;
+                    R32[r * m + c] = make_float2((float)v.x, (float)v.y);
+                }
             }
             __syncthreads();
             // X += Z R  (FP32 products on the FP32-rounded residual; FP64 update)
@@ -1195,8 +1250,8 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
                 const int c = rank + (idx / m) * CL, r = idx % m;
                 float ar = 0.f, ai = 0.f;
                 for (int k = 0; k < m; ++k) {
-                    const float2 zz = Z[r * m + k];
-                    const float xr = (float)R[k * m + c].x, xi = (float)R[k * m + c].y;
+                    const float2 zz = Z[r * w2 + k];
+                    const float xr = R32[k * m + c].x, xi = R32[k * m + c].y;
                     ar = fmaf(zz.x, xr, ar);
                     ar = fmaf(-zz.y, xi, ar);
                     ai = fmaf(zz.x, xi, ai);
