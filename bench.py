@@ -34,8 +34,12 @@ CONFIGS = {
 METRIC = "Krylov steps/s (pAMP x TensorPotential step, 1 GB300)"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
-# FP64 FMA issue rate measured on GB300 with a dependent-free FMA loop over all SMs
+# FMA issue rates measured on GB300 with dependency-free FMA loops over all SMs
 FP64_PEAK_TFLOPS = 1.195
+FP32_PEAK_TFLOPS = 69.9
+# DRAM bytes (read + write) per launch of the band kernel on the large workload, from one
+# ncu capture each (profiles/band_kernel_hydrogen_large.md)
+BAND_TRAFFIC = {"fp64": 20802560, "fp32-mixed": 20300288}
 
 
 def _dist():
@@ -137,17 +141,40 @@ def operator_slots(prob):
     return nslots, nterms
 
 
-def coef_bytes_of(prob, real_elem):
-    """Operator bytes one balanced matvec must read: the real band slots and the
-    parallel-solve tables of U^-1 and U^-T (diagonals, reciprocal diagonal,
-    coupling columns; the small scan operators are left out)."""
+def inverse_band_width(prob):
+    """Band width w of the approximate inverse of the overlap factor the solves apply
+    (same rule as the runtime: the dropped tail of every row below 2^-26 of the row)."""
+    rad = prob.psi.GetRepresentation().radial
+    n, kd = rad.count, rad.kd
+    Ub = rad.cholesky_band()
+    U = np.zeros((n, n))
+    for j in range(n):
+        for i in range(max(0, j - kd), j + 1):
+            U[i, j] = Ub[j * (kd + 1) + kd + i - j]
+    Ui = np.abs(np.linalg.inv(U))
+    W = min(n - 1, 160)
+    diag = np.stack([np.concatenate([np.diag(Ui, j), np.zeros(j)]) for j in range(W + 1)])
+    tot = diag.sum(0)
+    tail = np.cumsum(diag[::-1], axis=0)[::-1]           # tail[j] = sum_{j' >= j}
+    w = W
+    for j in range(W, 0, -1):
+        if (tail[j] / np.where(tot > 0, tot, 1)).max() > 2.0 ** -26:
+            break
+        w = j - 1
+    return w
+
+
+def coef_bytes_of(prob, precision):
+    """Operator bytes one balanced matvec reads once: the real band slots (FP64, or FP32
+    hi + lo for the mixed path: 8 bytes per coefficient either way) and, per solve, the
+    approximate-inverse band (FP32) and the factor's diagonals (FP64, or FP32 hi + lo)."""
     rad = prob.psi.GetRepresentation().radial
     nr, kd = rad.count, rad.kd
     nslots, _ = operator_slots(prob)
-    W = 2 * kd + 1
-    band = nslots * W * nr * real_elem
-    solve = 2 * (kd + 1 + kd) * nr * real_elem
-    return band, solve
+    band = nslots * (2 * kd + 1) * nr * 8
+    w = inverse_band_width(prob)
+    solve = 2 * ((w + 1) * nr * 4 + (kd + 1) * nr * 8)
+    return band, solve, w
 
 
 def build_problem(workload, precision, device):
@@ -313,6 +340,105 @@ def run_batch(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args, rank, world, local):
+    """Gradient of the final ground-state survival probability and of the total ionisation
+    probability with respect to 64 piecewise-linear field samples (seeded ~N(0.05, 0.01)):
+    l = 0..31 x 400 B-splines (linear breakpoints to 200 a.u.), m = 20, 1000 steps, forward
+    checkpoints every 50 steps.
+
+    timing (dt = 0.01): gradients/s in complex128 and complex64.  At this step the pAMP map
+    is numerically chaotic on this basis (||dt H_m|| reaches ~2^11; a 1e-16 relative change
+    of the initial state moves the survival probability by ~1e-5), which the line reports as
+    `forward_map_sensitivity`; finite differences cannot check a gradient there.
+    fd_check (dt = 0.0002, same sizes, where the discrete map is smooth): central
+    differences (h = 1e-6) against the adjoint, and the complex64 gradient against complex128."""
+    if rank != 0:
+        return
+    import torch
+    from pyprop_gb300 import _native
+    from pyprop_gb300.adjoint import AdjointPropagator, bound_states
+    from pyprop_gb300.batch import HydrogenProblem
+    device = "cuda:%d" % local
+    torch.cuda.set_device(local)
+    nsteps, nsamples = 1000, 64
+    rng = np.random.default_rng(20261205)
+    c = rng.normal(0.05, 0.01, nsamples)
+
+    def setup(dt):
+        prob = HydrogenProblem(lmax=31, nr=400, rmax=200.0, m=20, dt=dt, seed=20261205)
+        states, _, _ = bound_states(prob)
+        return prob, states, states[0].reshape(prob.nl, prob.nr)
+
+    prob, states, psi0 = setup(0.01)
+    ground = states[:1]
+    out = {"metric": "adjoint gradients/s (64 field samples, 1000 Krylov steps, 1 GB300)", "unit": "gradients/s",
+           "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+           "config": {"workload": "hydrogen_adjoint", "nl": prob.nl, "nr": prob.nr, "rmax": 200.0, "m": prob.m,
+                      "dt": 0.01, "steps": nsteps, "samples": nsamples, "checkpoint": 50,
+                      "bound_states": int(len(states))}}
+    for prec, name in ((_native.FP64, "c128"), (_native.FP32_MIXED, "c64")):
+        ap = AdjointPropagator(prob, nsteps, nsamples, checkpoint=50, precision=prec, device=device)
+        psi_T = ap.forward(psi0, c)                       # warm-up (graphs)
+        ap.gradient(psi_T, ground)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        psi_T = ap.forward(psi0, c)
+        ap.gradient(psi_T, ground)
+        torch.cuda.synchronize()
+        t_grad = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        psi_T = ap.forward(psi0, c, keep=False)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        out[name] = {"forward_s": t_fwd, "forward_plus_gradient_s": t_grad, "gradients_per_s": 1.0 / t_grad,
+                     "gradient_over_forward": t_grad / t_fwd}
+        if name == "c128":
+            surv = ap.observable(psi_T, ground)
+            pert = ap.observable(ap.forward(psi0 * (1 + 1e-16 * np.random.default_rng(1).standard_normal(psi0.shape)),
+                                            c, keep=False), ground)
+            out["forward_map_sensitivity"] = {"survival": surv, "d_survival_for_1e-16_relative_input_change":
+                                              pert - surv}
+    out["value"] = out["c128"]["gradients_per_s"]
+
+    # --- finite-difference and precision check where the discrete map is smooth -------------
+    dt_fd = 0.0002
+    prob, states, psi0 = setup(dt_fd)
+    ground = states[:1]
+    res = {"dt": dt_fd}
+    grads = {}
+    for prec, name in ((_native.FP64, "c128"), (_native.FP32_MIXED, "c64")):
+        ap = AdjointPropagator(prob, nsteps, nsamples, checkpoint=50, precision=prec, device=device)
+        psi_T = ap.forward(psi0, c)
+        g_s, _ = ap.gradient(psi_T, ground)
+        g_b, _ = ap.gradient(ap.forward(psi0, c), states)
+        grads[name] = (g_s, -g_b)
+        if name == "c128":
+            scale = float(np.abs(g_s).max())
+            for h in (1e-6, 1e-4):
+                fd = []
+                for k in (5, 31, 58):
+                    cp, cm = c.copy(), c.copy()
+                    cp[k] += h
+                    cm[k] -= h
+                    op_ = ap.observable(ap.forward(psi0, cp, keep=False), ground)
+                    om_ = ap.observable(ap.forward(psi0, cm, keep=False), ground)
+                    fd.append(((op_ - om_) / (2 * h), float(g_s[k])))
+                res["survival_fd_h%.0e" % h] = {"samples": [5, 31, 58], "fd": [f for f, _ in fd],
+                                                "adjoint": [a_ for _, a_ in fd],
+                                                "max_rel_err": max(abs(f - a_) for f, a_ in fd) / scale}
+            # noise floor of the observable: a 1e-16 relative change of the initial state
+            o0 = ap.observable(ap.forward(psi0, c, keep=False), ground)
+            o1 = ap.observable(ap.forward(psi0 * (1 + 1e-16 * np.random.default_rng(2).standard_normal(psi0.shape)),
+                                          c, keep=False), ground)
+            res["observable_noise"] = abs(o1 - o0)
+            res["fd_noise_rel_h1e-6"] = abs(o1 - o0) / (2e-6 * scale)
+    a_, b_ = grads["c128"], grads["c64"]
+    res["c64_vs_c128"] = {"survival_grad_rel_l2": float(np.linalg.norm(b_[0] - a_[0]) / np.linalg.norm(a_[0])),
+                          "ionisation_grad_rel_l2": float(np.linalg.norm(b_[1] - a_[1]) / np.linalg.norm(a_[1]))}
+    out["fd_check"] = res
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -320,10 +446,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbprop", choices=["gbprop", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32-mixed"])
-    ap.add_argument("--workload", default="large", choices=list(CONFIGS) + ["batch"])
+    ap.add_argument("--workload", default="large", choices=list(CONFIGS) + ["batch", "adjoint"])
     ap.add_argument("--batch-size", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--flush-mb", type=int, default=512)
+    ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed arm of the default run")
+    ap.add_argument("--no-precision-report", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -339,21 +467,48 @@ def main():
     if args.workload == "batch":
         run_batch(args, rank, world, local)
         return
+    if args.workload == "adjoint":
+        run_adjoint(args, rank, world, local)
+        return
 
     import torch
-    from pyprop_gb300 import _native
     device = "cuda:%d" % local
     torch.cuda.set_device(local)
+    main_arm = measure_single(args, args.precision, device, world, with_e2e=True)
+    line = main_arm.pop("line")
+    if args.precision == "fp64" and not args.no_mixed:
+        mixed = measure_single(args, "fp32-mixed", device, world, with_e2e=True)["line"]
+        line["fp32_mixed"] = {k: mixed[k] for k in ("value", "unit", "ms_per_step", "e2e", "roofline", "matvec_ms",
+                                                    "gpu_launches")}
+        line["fp32_mixed"]["speedup_vs_fp64"] = mixed["value"] / line["value"]
+        line["fp32_mixed"]["dtype"] = mixed["dtype"]
+    if not args.no_precision_report:
+        line["precision_report"] = precision_report(device)
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(args.workload)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
 
-    prob = build_problem(args.workload, args.precision, device)
+
+def measure_single(args, precision, device, world, with_e2e=True):
+    """One precision on the single-problem workload: device-resident steps/s (L2 flushed
+    between steps), e2e through the C ABI with host buffers, the band kernel alone and the
+    balanced matvec."""
+    import torch
+    from pyprop_gb300 import _native
+    prob = build_problem(args.workload, precision, device)
     h = prob.Propagator.Handle()
     nl, nr = prob.psi.GetRepresentation().GetFullShape()
     N = nl * nr
     m = prob.Propagator.BasisSize
-    elem = 16 if args.precision == "fp64" else 8
+    elem = 16 if precision == "fp64" else 8
     dt = prob.TimeStep
     bp = prob.Propagator.BasePropagator
     psi0 = prob.psi.GetData().clone()
+    local = torch.cuda.current_device()
 
     # --- device-resident timing: K steps, L2 flushed between steps ---------------------------
     flush = torch.empty(args.flush_mb * (1 << 20) // 4, dtype=torch.float32, device=device)
@@ -377,26 +532,28 @@ def main():
     torch.cuda.synchronize()
     _barrier(world)
     launches = _native.launch_count() - launches0
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms = sum(s_.elapsed_time(e) for s_, e in zip(starts, ends))
     clk = clocks.stop()
     ms = _max_over_ranks(ms, world)
     value = world * args.steps / (ms / 1e3)
 
     # --- e2e through the C ABI with host buffers (H2D psi, step, D2H psi per step) -----------
-    psi_host = np.ascontiguousarray(prob.psi.GetDataNumpy())
-    scal = np.array([bp._scaling(prob.PropagatedTime)])
-    for _ in range(2):
-        h.advance_host(psi_host, scal, dt)
-    _barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        h.advance_host(psi_host, scal, dt)
-    e2e_s = _max_over_ranks(time.perf_counter() - t0, world)
-    e2e = {"value": world * args.steps / e2e_s, "unit": "steps/s",
-           "h2d_bytes_per_step": psi_host.nbytes, "d2h_bytes_per_step": psi_host.nbytes}
+    e2e = None
+    if with_e2e:
+        psi_host = np.ascontiguousarray(prob.psi.GetDataNumpy())
+        scal = np.array([bp._scaling(prob.PropagatedTime)])
+        for _ in range(2):
+            h.advance_host(psi_host, scal, dt)
+        _barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            h.advance_host(psi_host, scal, dt)
+        e2e_s = _max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": world * args.steps / e2e_s, "unit": "steps/s",
+               "h2d_bytes_per_step": psi_host.nbytes, "d2h_bytes_per_step": psi_host.nbytes}
 
     # --- matvec alone: the tensor-potential kernel and the balanced matvec -------------------
-    band_coef, solve_coef = coef_bytes_of(prob, 8 if args.precision == "fp64" else 4)
+    band_coef, solve_coef, w = coef_bytes_of(prob, precision)
     B_mv, B_step = algorithmic_bytes(N, m, elem, band_coef + solve_coef)
     src = psi0.clone()
     dst = torch.empty_like(src)
@@ -418,29 +575,35 @@ def main():
     peak, peak_kind = load_peaks()
     band_bytes = 2 * N * elem + band_coef
     achieved = band_bytes / (t_band * 1e-3) / 1e9
-    # arithmetic of the band kernel: 2 FMA (4 flops) per real band entry per complex element
     _, nterms = operator_slots(prob)
-    band_flops = nterms * nr * (2 * prob.psi.GetRepresentation().radial.kd + 1) * 4
-    compute = {"unit": "TFLOP/s", "achieved": band_flops / (t_band * 1e-3) / 1e12,
-               "peak": FP64_PEAK_TFLOPS if args.precision == "fp64" else 69.9,
-               "peak_source": "measured FMA issue rate on GB300"}
+    kd = prob.psi.GetRepresentation().radial.kd
+    if precision == "fp64":
+        # 2 FMA (4 flops) per real band entry per complex element
+        band_flops = nterms * nr * (2 * kd + 1) * 4
+        compute = {"unit": "TFLOP/s", "achieved": band_flops / (t_band * 1e-3) / 1e12, "peak": FP64_PEAK_TFLOPS,
+                   "peak_source": "measured FP64 FMA issue rate on GB300", "what": "FP64 FMA"}
+    else:
+        # error-free products + compensated sums: ~22 FP32 ops per (hi, lo) band entry and component
+        band_flops = nterms * nr * (2 * kd + 1) * 2 * 22
+        compute = {"unit": "TFLOP/s", "achieved": band_flops / (t_band * 1e-3) / 1e12, "peak": FP32_PEAK_TFLOPS,
+                   "peak_source": "measured FP32 FMA issue rate on GB300", "what": "FP32 ops of the compensated sums"}
     compute["frac"] = compute["achieved"] / compute["peak"]
     roofline = {
-        "bound": "hbm", "kernel": "k_band_apply (TensorPotentialMultiply, all terms)",
+        "bound": "hbm", "kernel": "k_band_apply<%s> (TensorPotentialMultiply, all terms)" %
+                                  ("double" if precision == "fp64" else "float, hi/lo compensated"),
         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-        "traffic": None, "launch_ms": t_band,
+        "traffic": BAND_TRAFFIC.get(precision), "launch_ms": t_band,
         "algorithmic_bytes_per_launch": band_bytes,
         "compute": compute,
     }
-
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if precision == "fp64" else "c64+f64",
         "data": "synthetic",
         "config": {"workload": "hydrogen_velocity_%s" % args.workload, "nl": nl, "nr": nr, "order": 7, "m": m,
-                   "dt": dt.real, "precision": args.precision, "l2": "flushed between steps (%d MB write)" % args.flush_mb,
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "dt": dt.real, "precision": precision, "l2": "flushed between steps (%d MB write)" % args.flush_mb,
+                   "parallelism": "replicas" if world > 1 else "single", "inverse_band": w},
         "e2e": e2e,
         "roofline": roofline,
         "step_bytes": {"algorithmic_per_step": B_step, "achieved_GBps": B_step * value / world / 1e9,
@@ -449,13 +612,51 @@ def main():
         "clocks": clk,
         "gpu_launches": launches,
     }
-    if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(args.workload)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    del h, prob
+    torch.cuda.synchronize()
+    return {"line": line}
+
+
+def precision_report(device, nsteps=500):
+    """FP32-mixed against FP64 on the hydrogen workload of the small configuration
+    (l = 0..9 x 106 B-splines, m = 20, dt = 0.01, 500 steps): relative L2 of the final
+    state, bound-state populations and ionisation, for the seeded random initial state
+    of the workload and for the hydrogen ground state."""
+    import torch
+    import pyprop_gb300 as pp
+    from pyprop_gb300 import observables as ob
+    out = {"workload": "hydrogen_velocity_small", "steps": nsteps}
+    probs = {}
+    for prec in ("fp64", "fp32-mixed"):
+        conf = pp.Load(CONFIGS["small"])
+        conf.Propagation.Set("krylov_precision", prec)
+        pr = pp.Problem(conf, device=device)
+        pr.SetupStep()
+        probs[prec] = pr
+    p64 = probs["fp64"]
+    states, _, _ = ob.problem_bound_states(p64)
+    S = ob.radial_overlap(p64)
+    bp = p64.Propagator.BasePropagator
+    times, t = [], p64.PropagatedTime
+    for _ in range(nsteps):
+        times.append(t)
+        t = p64._next_time(t)
+    scal = np.array([bp._scaling(x) for x in times])
+    starts = {"random": p64.psi.GetDataNumpy().copy(), "ground": states[0].reshape(p64.psi.GetData().shape)}
+    for name, psi0 in starts.items():
+        res = {}
+        for prec, pr in probs.items():
+            dtp = torch.complex128 if prec == "fp64" else torch.complex64
+            d = torch.as_tensor(np.ascontiguousarray(psi0)).to(device, dtp)
+            pr.Propagator.Handle().advance(d, scal, pr.TimeStep)
+            res[prec] = d.cpu().numpy().astype(np.complex128)
+        a, b = res["fp64"], res["fp32-mixed"]
+        r64, r32 = ob.report(a, states, S), ob.report(b, states, S)
+        out[name] = {"rel_l2": float(np.linalg.norm(b - a) / np.linalg.norm(a)),
+                     "max_abs_d_population": float(np.abs(r64["populations"] - r32["populations"]).max()),
+                     "ionisation_fp64": r64["ionisation"], "ionisation_fp32_mixed": r32["ionisation"],
+                     "bound_fp64": r64["bound"], "bound_fp32_mixed": r32["bound"]}
+    return out
 
 
 if __name__ == "__main__":
