@@ -97,6 +97,10 @@ struct gbprop_ctx {
     void* d_y = nullptr;              // N, Krylov precision (H U^-1 v)
     double2* d_x = nullptr;           // N, complex128 (U psi, V y)
     double2* d_v0 = nullptr;          // N, complex128 first basis vector of a complex64 basis
+    int cgs_grid = 0;                 // > 0: Gram-Schmidt as one cooperative kernel of this many CTAs
+    int cgs_cache = 0;                // its V chunk cached in shared memory
+    double* d_cgs_part = nullptr;     // its partial sums
+    unsigned* d_gridbar = nullptr;    // its grid-barrier words
     std::vector<void*> allocs;
 
     cudaGraphExec_t graph = nullptr;      // one step on x (independent of the caller's buffers)
@@ -583,6 +587,8 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
     char* V = (char*)h->d_V;
     const size_t vbytes = (size_t)N * h->kelem();
     GB_LAUNCH(launch_step_begin(h->d_ctrl, h->d_H, m, s));
+    const bool fused = h->cgs_grid > 0 && !h->double_orth && h->expm_max_cluster > 1;
+    if (fused) GB_CUDA(cudaMemsetAsync(h->d_gridbar, 0, 2 * sizeof(unsigned), s));
     // beta0 = ||x||
     GB_LAUNCH(launch_norm(0, h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
     for (int J = 0; J < m; ++J) {
@@ -598,6 +604,11 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
         // w = U^-T y
         GB_LAUNCH(ksolve(h, 1, h->d_y, kp, h->d_r, kp, nullptr, kp, 0, 1));
         // classical Gram-Schmidt against v_0..v_J
+        if (fused) {
+            GB_LAUNCH(launch_arnoldi_cgs(kp, V, h->d_v0, N, J, m, h->d_r, h->d_cgs_part, h->d_gridbar, h->d_ctrl,
+                                         h->d_H, J < m - 1, h->cgs_grid, h->cgs_cache, s));
+            continue;
+        }
         GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0,
                                  h->double_orth, s));
         if (J < m - 1 || h->double_orth)
@@ -831,6 +842,26 @@ gbprop_status gbprop_finalize(gbprop_handle h) {
     if ((st = h->dalloc(&h->d_y, (size_t)h->N * ke))) return st;
     if ((st = h->dalloc(&h->d_x, (size_t)h->N * sizeof(double2)))) return st;
     if (h->prec != GBPROP_FP64 && (st = h->dalloc(&h->d_v0, (size_t)h->N * sizeof(double2)))) return st;
+    // cooperative Gram-Schmidt (single handles; GBPROP_CGS=separate keeps the three-kernel form)
+    {
+        const char* env = std::getenv("GBPROP_CGS");
+        const bool allow = !(env && std::strcmp(env, "separate") == 0) && !h->double_orth;
+        const int kpv = h->kprec(), with_v0 = h->d_v0 != nullptr;
+        int grid = allow ? arnoldi_cgs_grid(kpv, h->N, h->m, with_v0, 1) : 0;
+        int cache = 1;
+        if (allow && grid == 0) {
+            grid = arnoldi_cgs_grid(kpv, h->N, h->m, with_v0, 0);
+            cache = 0;
+        }
+        cudaGetLastError();
+        if (grid > 0) {
+            if ((st = h->dalloc(&h->d_cgs_part, arnoldi_cgs_part_doubles(grid) * sizeof(double)))) return st;
+            if ((st = h->dalloc(&h->d_gridbar, 64))) return st;
+            GB_CUDA(cudaMemsetAsync(h->d_gridbar, 0, 64, h->stream));
+            h->cgs_grid = grid;
+            h->cgs_cache = cache;
+        }
+    }
     if ((st = ensure_sched(h, 1024))) return st;
     GB_CUDA(cudaStreamSynchronize(h->stream));
     h->finalized = true;

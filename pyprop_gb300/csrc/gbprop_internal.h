@@ -187,6 +187,17 @@ cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const vo
 cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, long n, int nv, void* w, double* partials,
                               unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
 cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, cudaStream_t s);
+// One Arnoldi step's Gram-Schmidt (dot, update, norm, Hessenberg column, breakdown) as a
+// single cooperative kernel of `grid` co-resident CTAs (gbprop_cgs.cu).  part: at least
+// arnoldi_cgs_part_doubles(grid) doubles; bar: two words, zero before the first launch.
+// update = 0 forms only the Hessenberg column (last vector).  cache: keep V's chunk in
+// shared memory between the two passes.
+cudaError_t launch_arnoldi_cgs(int prec, const void* V, const double2* v0, long n, int J, int m, void* w,
+                               double* part, unsigned* bar, Ctrl* ctrl, double* H, int update, int grid, int cache,
+                               cudaStream_t s);
+// Grid size for the cooperative Gram-Schmidt (0 if it cannot run co-resident).
+int arnoldi_cgs_grid(int prec, long n, int m, int with_v0, int cache);
+inline size_t arnoldi_cgs_part_doubles(int grid) { return (size_t)(2 * (kMaxBasis + 1) + 1) * grid; }
 cudaError_t launch_step_begin(Ctrl* ctrl, double* H, int m, cudaStream_t s);
 // max_cluster: 16 lets one problem's exponential spread over a thread-block cluster; 1 keeps it on
 // one CTA (batches, where other problems fill the GPU).

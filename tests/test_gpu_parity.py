@@ -98,6 +98,26 @@ def test_solver_choice_vs_oracle(solver, monkeypatch):
     assert rel(_host(d), want) < 1e-12
 
 
+@pytest.mark.parametrize("form", ["cooperative", "separate"])
+def test_gram_schmidt_forms_vs_oracle(form, monkeypatch):
+    """Both Gram-Schmidt forms (one cooperative kernel per Arnoldi step, default for a single
+    handle; dot / update / finalize kernels, GBPROP_CGS=separate) give the oracle's
+    propagation, including the last basis vector and the Hessenberg matrix."""
+    monkeypatch.setenv("GBPROP_CGS", form)
+    prob = make_problem(maxl=6, xsize=80, m=14)
+    op = orc.Operator.from_problem(prob)
+    psi0 = prob.psi.GetDataNumpy().copy()
+    scal = list(np.linspace(0.1, 0.4, 8))
+    want, _ = op.advance(psi0, 14, prob.TimeStep, scal)
+    d = _dev(psi0)
+    h = prob.Propagator.Handle()
+    h.reset_stats()
+    h.advance(d, scal, prob.TimeStep)
+    assert rel(_host(d), want) < 1e-12
+    st = h.stats()
+    assert st.operator_count == 14 * len(scal) and st.last_basis_size == 14
+
+
 def test_stateless_tensor_multiply_vs_oracle(small):
     from pyprop_gb300 import _native
     L = _native.lib()
