@@ -603,7 +603,8 @@ def measure_single(args, precision, device, world, with_e2e=True):
         "data": "synthetic",
         "config": {"workload": "hydrogen_velocity_%s" % args.workload, "nl": nl, "nr": nr, "order": 7, "m": m,
                    "dt": dt.real, "precision": precision, "l2": "flushed between steps (%d MB write)" % args.flush_mb,
-                   "parallelism": "replicas" if world > 1 else "single", "inverse_band": w},
+                   "parallelism": "replicas" if world > 1 else "single", "inverse_band": w,
+                   "band_variant": prob.Propagator.BandVariant},
         "e2e": e2e,
         "roofline": roofline,
         "step_bytes": {"algorithmic_per_step": B_step, "achieved_GBps": B_step * value / world / 1e9,

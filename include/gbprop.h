@@ -139,7 +139,9 @@ gbprop_status gbprop_synchronize(gbprop_handle h);
 
 /* Band-kernel tile autotuner: times every tile shape of the TensorPotential matvec
  * kernel on this handle's operator and keeps the fastest; *variant (if not NULL)
- * receives its index.  Synchronises the handle's stream. */
+ * receives its index.  Synchronises the handle's stream.  If *variant >= 0 on entry,
+ * that shape is selected without timing (GBPROP_EINVAL if it does not exist).
+ * No counterpart in the reference (its generated kernels have one shape). */
 gbprop_status gbprop_autotune(gbprop_handle h, int* variant);
 
 /* Batches of independent problems (each a finalized handle, all of one precision,

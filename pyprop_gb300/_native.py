@@ -200,8 +200,10 @@ class Handle:
     def synchronize(self):
         check(lib().gbprop_synchronize(self._h))
 
-    def autotune(self):
-        v = C.c_int(-1)
+    def autotune(self, variant=-1):
+        """Time the band kernel's tile shapes and keep the fastest (variant < 0), or select
+        `variant`; returns the shape in use."""
+        v = C.c_int(int(variant))
         check(lib().gbprop_autotune(self._h, C.byref(v)))
         return v.value
 

@@ -1013,6 +1013,11 @@ gbprop_status gbprop_tensor_multiply_bandnh(int storage, const void* V, int npai
 
 gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
     if (gbprop_status st = check_handle(h, true)) return st;
+    if (variant && *variant >= 0) {                  // explicit choice, no timing
+        if (*variant >= band_variant_count()) return fail(GBPROP_EINVAL, "no such band-kernel variant");
+        set_band_variant(h, *variant);
+        return GBPROP_OK;
+    }
     const int kp = h->kprec();
     cudaStream_t s = h->stream;
     cudaEvent_t e0, e1;

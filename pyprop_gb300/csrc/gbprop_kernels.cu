@@ -146,8 +146,11 @@ __device__ void block_partials<16>(double (&acc)[16], int nvalid, double* partia
 // ---------------------------------------------------------------------------
 // Tile shapes of the band kernel the autotuner chooses between:
 // (threads per block, radial elements per thread).
-constexpr int kBandVariants = 4;
-__host__ __device__ constexpr int band_threads(int v) { return v == 0 ? 64 : v == 1 ? 128 : v == 2 ? 128 : 256; }
+// Variants 4 and 5 stage nothing: one thread per element reads its stencil through L1.
+constexpr int kBandVariants = 6;
+__host__ __device__ constexpr int band_threads(int v) {
+    return v == 0 ? 64 : v == 1 ? 128 : v == 2 ? 128 : v == 3 ? 256 : v == 4 ? 128 : 256;
+}
 __host__ __device__ constexpr int band_per(int v) { return v == 0 ? 2 : v == 1 ? 2 : v == 2 ? 4 : 1; }
 
 // One block: destination row l = blockIdx.y, radial tile blockIdx.x.  For every term
@@ -264,9 +267,92 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
     }
 }
 
+// Unstaged form: thread = (row l, element i); every term's 2kb+1 source values come
+// through the read-only/L1 path (a source element is shared by 2kb+1 neighbouring threads),
+// so no block barrier ever waits on a global load.
+template <typename T, int KB, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_band_apply_l1(BandOp<T> op, const cx<T>* __restrict__ x,
+                                                           cx<T>* __restrict__ y, const SchedEntry* __restrict__ sched,
+                                                           const Ctrl* __restrict__ ctrl, double scal_val,
+                                                           int check_broken) {
+    using C = cx<T>;
+    constexpr int W = 2 * KB + 1;
+    if (check_broken && ctrl->broken) return;
+    const int l = blockIdx.y, nr = op.nr;
+    const int i = blockIdx.x * THREADS + threadIdx.x;
+    if (i >= nr) return;
+    const double scal = sched ? sched[ctrl->step].scaling : scal_val;
+    const bool split = sizeof(T) < sizeof(double) && op.slots_lo != nullptr;
+    T yr = 0, yi = 0, zr = 0, zi = 0;
+    const int t0 = op.row_ptr[l], t1 = op.row_ptr[l + 1];
+    for (int t = t0; t < t1; ++t) {
+        const C* xs = x + (size_t)op.t_src[t] * nr;
+        const T* A = op.slots + (size_t)op.t_slot[t] * W * nr;
+        double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
+        if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
+        const T Cr = (T)cr, Ci = (T)ci;
+        C v[W];
+#pragma unroll
+        for (int d = 0; d < W; ++d) {
+            const int g = i + d - KB;
+            v[d] = (g >= 0 && g < nr) ? __ldg(xs + g) : mk<T>(0, 0);
+        }
+        if constexpr (sizeof(T) < sizeof(double)) {
+            if (split) {
+                const float* Alo = op.slots_lo + (size_t)op.t_slot[t] * W * nr;
+                const float Crl = (float)(cr - (double)Cr), Cil = (float)(ci - (double)Ci);
+                float srh = 0.f, srl = 0.f, sih = 0.f, sil = 0.f, orh = 0.f, orl = 0.f, oih = 0.f, oil = 0.f;
+#pragma unroll
+                for (int d = 0; d < W; ++d) {
+                    const float a = __ldg(A + (size_t)d * nr + i), al = __ldg(Alo + (size_t)d * nr + i);
+                    if (d & 1) {
+                        acc_prod(orh, orl, a, al, v[d].x);
+                        acc_prod(oih, oil, a, al, v[d].y);
+                    } else {
+                        acc_prod(srh, srl, a, al, v[d].x);
+                        acc_prod(sih, sil, a, al, v[d].y);
+                    }
+                }
+                float tt;
+                two_sum(srh, orh, srh, tt);
+                srl = __fadd_rn(__fadd_rn(srl, orl), tt);
+                two_sum(sih, oih, sih, tt);
+                sil = __fadd_rn(__fadd_rn(sil, oil), tt);
+                if (Cr != 0.f || Crl != 0.f) {
+                    acc_scaled(yr, zr, Cr, Crl, srh, srl);
+                    acc_scaled(yi, zi, Cr, Crl, sih, sil);
+                }
+                if (Ci != 0.f || Cil != 0.f) {
+                    acc_scaled(yr, zr, -Ci, -Cil, sih, sil);
+                    acc_scaled(yi, zi, Ci, Cil, srh, srl);
+                }
+                continue;
+            }
+        }
+        T ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
+#pragma unroll
+        for (int d = 0; d < W; ++d) {
+            const T a = __ldg(A + (size_t)d * nr + i);
+            if (d & 1) { ar1 = fma(a, v[d].x, ar1); ai1 = fma(a, v[d].y, ai1); }
+            else { ar0 = fma(a, v[d].x, ar0); ai0 = fma(a, v[d].y, ai0); }
+        }
+        const T ar = ar0 + ar1, ai = ai0 + ai1;
+        yr += Cr * ar - Ci * ai;
+        yi += Cr * ai + Ci * ar;
+    }
+    y[(size_t)l * nr + i] = mk<T>(yr + zr, yi + zi);
+}
+
 template <typename T, int KB, int V>
 static void band_apply_v(const BandOp<T>& op, const void* x, void* y, const SchedEntry* sched, const Ctrl* ctrl,
                          double scaling, int check_broken, cudaStream_t s) {
+    if constexpr (V >= 4) {
+        constexpr int TH = band_threads(V);
+        dim3 grid((op.nr + TH - 1) / TH, op.nl);
+        k_band_apply_l1<T, KB, TH><<<grid, TH, 0, s>>>(op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl, scaling,
+                                                       check_broken);
+        return;
+    }
     constexpr int TH = band_threads(V), PE = band_per(V);
     dim3 grid((op.nr + TH * PE - 1) / (TH * PE), op.nl);
     k_band_apply<T, KB, TH, PE><<<grid, TH, 0, s>>>(op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl, scaling, check_broken);
@@ -279,6 +365,8 @@ static void band_apply_kb(const BandOp<T>& op, const void* x, void* y, const Sch
         case 0: band_apply_v<T, KB, 0>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
         case 2: band_apply_v<T, KB, 2>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
         case 3: band_apply_v<T, KB, 3>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
+        case 4: band_apply_v<T, KB, 4>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
+        case 5: band_apply_v<T, KB, 5>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
         default: band_apply_v<T, KB, 1>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
     }
 }

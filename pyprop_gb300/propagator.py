@@ -178,6 +178,8 @@ class PamPropagator(PropagatorBase):
         self.ExponentiationMethod = 0
         self.DoubleOrthogonalization = False
         self.Precision = _native.FP64
+        self.Autotune = True
+        self.BandVariant = None
         self._handle = None
         self.PampWrapper = _PampCounters(self)
 
@@ -197,12 +199,17 @@ class PamPropagator(PropagatorBase):
             self.DoubleOrthogonalization = bool(sec.krylov_double_orthogonalization)
         if hasattr(sec, "krylov_precision"):
             self.Precision = precision_of(sec.krylov_precision)
+        if hasattr(sec, "krylov_autotune"):
+            self.Autotune = bool(sec.krylov_autotune)
 
     def SetupStep(self, dt):
         self.BasePropagator.SetupStep(dt)
         _require_device(self.psi)
         self._handle = build_handle(self.psi, self.BasePropagator.PotentialList, self.Precision, self.BasisSize,
                                     self.ExponentiationMethod, self.DoubleOrthogonalization)
+        if self.Autotune:
+            # pick the band kernel's tile shape for this operator
+            self.BandVariant = self._handle.autotune()
         self.BasePropagator.AttachHandle(self._handle)
         self.TempPsi = self.psi.CopyDeep()
 

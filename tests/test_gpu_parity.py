@@ -118,6 +118,28 @@ def test_gram_schmidt_forms_vs_oracle(form, monkeypatch):
     assert st.operator_count == 14 * len(scal) and st.last_basis_size == 14
 
 
+@pytest.mark.parametrize("variant", range(6))
+@pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
+def test_band_kernel_variants(variant, precision):
+    """Every tile shape of the band kernel (staged tiles and the unstaged L1 form) applies the
+    reference-storage operator: FP64 to the oracle's rounding, complex64 to one rounding of
+    the exact result (hi/lo coefficients, compensated sums)."""
+    from pyprop_gb300 import _native
+    prob = make_problem(maxl=5, xsize=300, m=4, precision=precision)
+    op = orc.Operator.from_problem(prob)
+    rng = np.random.default_rng(31)
+    x = rng.standard_normal((op.nl, op.nr)) + 1j * rng.standard_normal((op.nl, op.nr))
+    h = prob.Propagator.Handle()
+    assert h.autotune(variant) == variant
+    torch = _torch()
+    dt = torch.complex128 if precision == "fp64" else torch.complex64
+    src = _dev(x.astype(np.complex64) if precision != "fp64" else x, dt)
+    dst = torch.zeros_like(src)
+    h.matvec(src, dst, 0.37, balanced=False)
+    want = op.multiply_potentials(_host(src).astype(np.complex128), 0.37)
+    assert rel(_host(dst).astype(np.complex128), want) < (1e-14 if precision == "fp64" else 1e-7)
+
+
 def test_stateless_tensor_multiply_vs_oracle(small):
     from pyprop_gb300 import _native
     L = _native.lib()
