@@ -137,6 +137,29 @@ gbprop_status gbprop_reset_stats(gbprop_handle h);
 gbprop_status gbprop_get_hessenberg(gbprop_handle h, double* out);
 gbprop_status gbprop_synchronize(gbprop_handle h);
 
+/* Statistics of one gbprop_expokit_advance call (Expokit's zgexpv diagnostics). */
+typedef struct {
+    long long substeps;      /* accepted Krylov sub-steps */
+    long long rejections;    /* rejected sub-step sizes */
+    long long matvecs;       /* operator applications */
+    double error;            /* sum of the local error estimates */
+    double hump;             /* max ||w|| over the sub-steps / ||w_0|| (conditioning measure) */
+    double last_step;        /* last accepted sub-step size */
+} gbprop_expokit_stats;
+
+/* ExpokitPropagator.AdvanceStep (pyprop/propagator/KrylovPropagator.py:44-49 ->
+ * core/krylov/expokit/expokitpropagator.cpp:36-103 -> Expokit zgexpv): nsteps steps of size
+ * |dt|, each psi <- U^-1 exp(-i |dt| A) U psi (imaginary dt: exp(-|dt| A)), A the balanced
+ * operator at scalings[k] (fixed within step k, as the reference's callback fixes the step's
+ * start time), evaluated by Krylov sub-steps with local error control.  The Krylov dimension
+ * is the handle's krylov_basis_size - 1 (a handle for Expokit holds m + 1 vectors); tol and
+ * anorm are krylov_tolerance and krylov_norm.  stats may be NULL.  Host-driven (the sub-step
+ * sizes depend on the error estimates); returns after the work is enqueued and the last
+ * sub-step decision is taken. */
+gbprop_status gbprop_expokit_advance(gbprop_handle h, void* psi, int nsteps, const double* scalings,
+                                     double dt_re, double dt_im, double tol, double anorm,
+                                     gbprop_expokit_stats* stats);
+
 /* Band-kernel tile autotuner: times every tile shape of the TensorPotential matvec
  * kernel on this handle's operator and keeps the fastest; *variant (if not NULL)
  * receives its index.  Synchronises the handle's stream.  If *variant >= 0 on entry,

@@ -522,3 +522,182 @@ int orc_pamp_once(const orc_operator* op, cplx* x, int m, double dt_re, double d
     free(V); free(r); free(tmp); free(work);
     return rc;
 }
+
+
+/* ------------------------------------------------------------------------ */
+/* ExpokitPropagator (pyprop/propagator/KrylovPropagator.py:44-49,           */
+/* core/krylov/expokit/expokitpropagator.cpp:36-103): Expokit zgexpv with the */
+/* balanced matvec times -i (real time) or -1 (imaginary time),              */
+/* core/krylov/krylovcommon.h:61-70.  Restated from the published algorithm  */
+/* (Sidje, ACM TOMS 24, 1998) as the reference calls it: modified Gram-      */
+/* Schmidt Arnoldi on the operator itself, augmented (m+2) Hessenberg,       */
+/* zgpadm Pade (6,6) scaled by the infinity norm, two-term error estimate,   */
+/* step sizes rounded to two significant digits.                            */
+/* ------------------------------------------------------------------------ */
+
+/* zgpadm: exp(t H), H n x n row-major, into E; returns LU info. */
+static int expokit_pade(int n, const cplx* H, double t, cplx* E) {
+    const int p = 6;
+    long nn = (long)n * n;
+    double hn = 0.0;
+    for (int i = 0; i < n; i++) {
+        double r = 0.0;
+        for (int j = 0; j < n; j++) { cplx v = H[i * n + j]; r += sqrt(v.re * v.re + v.im * v.im); }
+        if (r > hn) hn = r;
+    }
+    hn = fabs(t * hn);
+    if (hn == 0.0) {
+        memset(E, 0, nn * sizeof(cplx));
+        for (int i = 0; i < n; i++) E[i * n + i].re = 1.0;
+        return 0;
+    }
+    int ns = (int)(log(hn) / log(2.0)) + 2;
+    if (ns < 0) ns = 0;
+    double sc = t / ldexp(1.0, ns), sc2 = sc * sc;
+    double c[8];
+    c[0] = 1.0;
+    for (int k = 1; k <= p; k++) c[k] = c[k - 1] * (double)(p + 1 - k) / (double)(k * (2 * p + 1 - k));
+    cplx* H2 = (cplx*)calloc(nn, sizeof(cplx));
+    cplx* P = (cplx*)calloc(nn, sizeof(cplx));
+    cplx* Q = (cplx*)calloc(nn, sizeof(cplx));
+    cplx* T = (cplx*)calloc(nn, sizeof(cplx));
+    mat_mul(n, H, H, H2);
+    for (long i = 0; i < nn; i++) { H2[i].re *= sc2; H2[i].im *= sc2; }
+    for (int i = 0; i < n; i++) { P[i * n + i].re = c[p - 1]; Q[i * n + i].re = c[p]; }
+    int odd = 1;
+    for (int k = p - 1; k > 0; k--) {
+        cplx* X = odd ? Q : P;
+        mat_mul(n, X, H2, T);
+        memcpy(X, T, nn * sizeof(cplx));
+        for (int i = 0; i < n; i++) X[i * n + i].re += c[k - 1];
+        odd = 1 - odd;
+    }
+    cplx* X = odd ? Q : P;
+    mat_mul(n, X, H, T);
+    for (long i = 0; i < nn; i++) { X[i].re = sc * T[i].re; X[i].im = sc * T[i].im; }
+    for (long i = 0; i < nn; i++) Q[i] = csub(Q[i], P[i]);
+    int info = lu_solve(n, Q, P);
+    for (long i = 0; i < nn; i++) { E[i].re = 2.0 * P[i].re; E[i].im = 2.0 * P[i].im; }
+    for (int i = 0; i < n; i++) E[i * n + i].re += 1.0;
+    if (ns == 0 && odd) {
+        for (long i = 0; i < nn; i++) { E[i].re = -E[i].re; E[i].im = -E[i].im; }
+    } else {
+        for (int k = 0; k < ns; k++) { mat_mul(n, E, E, T); memcpy(E, T, nn * sizeof(cplx)); }
+    }
+    free(H2); free(P); free(Q); free(T);
+    return info;
+}
+
+static double expokit_round(double x) {
+    int e = (int)lround(log10(x) - sqrt(0.1)) - 1;
+    double p = pow(10.0, (double)e);
+    return trunc(x / p + 0.55) * p;
+}
+
+typedef struct {
+    long substeps, rejections, matvecs;
+    double error, hump, last_step;
+} orc_expokit_stats;
+
+/* zgexpv on w (balanced coordinates, in place): w <- exp(t_out * fac * A) w. */
+static int zgexpv(const orc_operator* op, double scaling, int m, double t_out, cplx fac, double tol, double anorm,
+                  cplx* w, cplx* V, cplx* work, orc_expokit_stats* st) {
+    long N = (long)op->nl * op->nr;
+    int mh = m + 2;
+    cplx* H = (cplx*)calloc((long)mh * mh, sizeof(cplx));
+    cplx* F = (cplx*)calloc((long)mh * mh, sizeof(cplx));
+    cplx* Hs = (cplx*)calloc((long)mh * mh, sizeof(cplx));
+    double eps = DBL_EPSILON;
+    if (tol <= eps) tol = sqrt(eps);
+    double rndoff = eps * anorm, btol = 1e-7;
+    double beta = global_norm(N, w), vnorm = beta;
+    double xm = 1.0 / m;
+    double p2 = tol * pow((m + 1) / 2.72, m + 1) * sqrt((m + 1) * 6.28);
+    double t_new = expokit_round(1.0 / anorm * pow(p2 / (4.0 * beta * anorm), xm));
+    double t_now = 0.0;
+    int rc = 0;
+    while (t_now < t_out) {
+        double t_step = t_out - t_now < t_new ? t_out - t_now : t_new;
+        for (long i = 0; i < N; i++) { V[i].re = w[i].re / beta; V[i].im = w[i].im / beta; }
+        memset(H, 0, (long)mh * mh * sizeof(cplx));
+        int k1 = 2, mb = m;
+        double avnorm = 0.0;
+        for (int j = 0; j < m; j++) {
+            cplx* p = V + (long)(j + 1) * N;
+            orc_balanced_matvec(op, scaling, V + (long)j * N, p, work);
+            for (long i = 0; i < N; i++) p[i] = cmul(fac, p[i]);
+            st->matvecs++;
+            for (int i = 0; i <= j; i++) {                   /* modified Gram-Schmidt */
+                cplx hij = zdotc(N, V + (long)i * N, p);
+                zaxpy(N, (cplx){-hij.re, -hij.im}, V + (long)i * N, p);
+                H[i * mh + j] = hij;
+            }
+            double hj1j = global_norm(N, p);
+            if (hj1j <= btol) { k1 = 0; mb = j + 1; t_step = t_out - t_now; break; }
+            H[(j + 1) * mh + j].re = hj1j;
+            zscal(N, (cplx){1.0 / hj1j, 0.0}, p);
+        }
+        if (k1 != 0) {
+            orc_balanced_matvec(op, scaling, V + (long)m * N, work + N, work);
+            for (long i = 0; i < N; i++) work[N + i] = cmul(fac, work[N + i]);
+            st->matvecs++;
+            avnorm = global_norm(N, work + N);
+            H[(m + 1) * mh + m].re = 1.0;
+        }
+        int ireject = 0, mx;
+        double err_loc = 0.0;
+        for (;;) {
+            mx = mb + k1;
+            for (int i = 0; i < mx; i++) for (int j = 0; j < mx; j++) Hs[i * mx + j] = H[i * mh + j];
+            if (expokit_pade(mx, Hs, t_step, F)) { rc = 1; goto done; }
+            if (k1 == 0) { err_loc = tol; break; }
+            double q1 = sqrt(F[m * mx].re * F[m * mx].re + F[m * mx].im * F[m * mx].im) * beta;
+            double q2 = sqrt(F[(m + 1) * mx].re * F[(m + 1) * mx].re + F[(m + 1) * mx].im * F[(m + 1) * mx].im) * beta * avnorm;
+            if (q1 > 10.0 * q2) { err_loc = q2; xm = 1.0 / m; }
+            else if (q1 > q2) { err_loc = q1 * q2 / (q1 - q2); xm = 1.0 / m; }
+            else { err_loc = q1; xm = 1.0 / (m - 1); }
+            if (err_loc <= 1.2 * t_step * tol) break;
+            t_step = expokit_round(0.9 * t_step * pow(t_step * tol / err_loc, xm));
+            st->rejections++;
+            if (++ireject > 100) { rc = 2; goto done; }
+        }
+        mx = mb + (k1 - 1 > 0 ? k1 - 1 : 0);
+        {
+            int ld = mb + k1;
+            memset(w, 0, N * sizeof(cplx));
+            for (int k = 0; k < mx; k++) {
+                cplx f = { beta * F[k * ld].re, beta * F[k * ld].im };
+                zaxpy(N, f, V + (long)k * N, w);
+            }
+        }
+        beta = global_norm(N, w);
+        if (beta / vnorm > st->hump) st->hump = beta / vnorm;
+        t_now += t_step;
+        t_new = expokit_round(0.9 * t_step * pow(t_step * tol / err_loc, xm));
+        st->error += err_loc > rndoff ? err_loc : rndoff;
+        st->last_step = t_step;
+        st->substeps++;
+    }
+done:
+    free(H); free(F); free(Hs);
+    return rc;
+}
+
+int orc_expokit_advance(const orc_operator* op, cplx* psi, int m, double dt_re, double dt_im, int nsteps,
+                        const double* scalings, double tol, double anorm, orc_expokit_stats* st) {
+    long N = (long)op->nl * op->nr;
+    cplx* V = (cplx*)malloc(sizeof(cplx) * (long)(m + 1) * N);
+    cplx* work = (cplx*)malloc(sizeof(cplx) * 2 * N);
+    double t_out = sqrt(dt_re * dt_re + dt_im * dt_im);
+    cplx fac = fabs(dt_im) > 1e-10 ? (cplx){-1.0, 0.0} : (cplx){0.0, -1.0};
+    int rc = 0;
+    st->substeps = st->rejections = st->matvecs = 0;
+    st->error = 0.0; st->hump = 1.0; st->last_step = 0.0;
+    for (int n = 0; n < nsteps && !rc; n++) {
+        orc_multiply_sqrt_overlap(op, psi);
+        rc = zgexpv(op, scalings[n], m, t_out, fac, tol, anorm, psi, V, work, st);
+        orc_solve_sqrt_overlap(op, 0, psi);
+    }
+    free(V); free(work);
+    return rc;
+}

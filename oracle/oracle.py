@@ -87,6 +87,9 @@ def lib():
         L.orc_pamp_once.argtypes = [C.POINTER(OrcOperator), P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
                                     P, C.POINTER(OrcStats)]
         L.orc_pamp_once.restype = C.c_int
+        L.orc_expokit_advance.argtypes = [C.POINTER(OrcOperator), P, C.c_int, C.c_double, C.c_double, C.c_int, P,
+                                          C.c_double, C.c_double, C.POINTER(OrcExpokitStats)]
+        L.orc_expokit_advance.restype = C.c_int
         _lib = L
     return _lib
 
@@ -127,6 +130,17 @@ def scaling_pade_exponential(A, order=6):
     s = C.c_int(0)
     info = lib().orc_scaling_pade_exponential(m, _p(A), order, _p(out), C.byref(s))
     return out, info, s.value
+
+
+class OrcExpokitStats(C.Structure):
+    _fields_ = [
+        ("substeps", C.c_long),
+        ("rejections", C.c_long),
+        ("matvecs", C.c_long),
+        ("error", C.c_double),
+        ("hump", C.c_double),
+        ("last_step", C.c_double),
+    ]
 
 
 class Operator:
@@ -214,6 +228,18 @@ class Operator:
                                int(bool(double_orth)), C.byref(st))
         if rc:
             raise RuntimeError("oracle Pade LU failed (info %d)" % rc)
+        return x, st
+
+    def expokit_advance(self, psi, m, dt, scalings, tol, anorm):
+        """len(scalings) ExpokitPropagator steps (zgexpv, Krylov dimension m); returns (psi, stats)."""
+        x = self._vec(psi)
+        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        st = OrcExpokitStats()
+        dt = complex(dt)
+        rc = lib().orc_expokit_advance(C.byref(self.op), _p(x), int(m), dt.real, dt.imag, len(s), _p(s),
+                                       float(tol), float(anorm), C.byref(st))
+        if rc:
+            raise RuntimeError("oracle Expokit failed (%d)" % rc)
         return x, st
 
     def pamp_once(self, x, m, dt, scaling, double_orth=False):

@@ -8,14 +8,14 @@ from .config import Config, Load, LoadString, Section
 from .initial import GaussianRandomState
 from .potentials import LaserFunctionSimpleLength, LaserFunctionVelocity, PiecewiseLinearField
 from .problem import InitialConditionType, LoadPropagator, Problem
-from .propagator import BasisPropagator, PamPropagator, PropagatorBase
+from .propagator import BasisPropagator, ExpokitPropagator, PamPropagator, PropagatorBase
 from .representation import (BSplineRepresentation, CombinedRepresentation, ReducedSphericalHarmonicRepresentation,
                              Wavefunction)
 from .tensorpotential import TensorPotential
 from .namespace import PotentialType
 
 __all__ = [
-    "Config", "Load", "LoadString", "Section", "Problem", "LoadPropagator", "PamPropagator", "BasisPropagator",
+    "Config", "Load", "LoadString", "Section", "Problem", "LoadPropagator", "PamPropagator", "ExpokitPropagator", "BasisPropagator",
     "PropagatorBase", "TensorPotential", "Wavefunction", "CombinedRepresentation", "BSplineRepresentation",
     "ReducedSphericalHarmonicRepresentation", "InitialConditionType", "PotentialType", "LaserFunctionVelocity",
     "LaserFunctionSimpleLength", "PiecewiseLinearField", "GaussianRandomState",

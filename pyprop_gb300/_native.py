@@ -42,6 +42,17 @@ class Stats(C.Structure):
     ]
 
 
+class ExpokitStats(C.Structure):
+    _fields_ = [
+        ("substeps", C.c_longlong),
+        ("rejections", C.c_longlong),
+        ("matvecs", C.c_longlong),
+        ("error", C.c_double),
+        ("hump", C.c_double),
+        ("last_step", C.c_double),
+    ]
+
+
 _lib = None
 
 # name -> (restype, argtypes)
@@ -66,6 +77,8 @@ _PROTOS = {
     "gbprop_tensor_multiply_bandnh": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double,
                                                 C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "gbprop_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "gbprop_expokit_advance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_double,
+                                         C.c_double, C.c_double, C.POINTER(ExpokitStats)]),
     "gbprop_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_void_p]),
     "gbprop_batch_advance": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.c_void_p]),
     "gbprop_batch_destroy": (C.c_int, [C.c_void_p]),
@@ -199,6 +212,16 @@ class Handle:
 
     def synchronize(self):
         check(lib().gbprop_synchronize(self._h))
+
+    def expokit_advance(self, psi_dev, scalings, dt, tol, anorm):
+        """Expokit steps (Krylov dimension = this handle's basis size - 1); returns ExpokitStats."""
+        import numpy as np
+        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        dt = complex(dt)
+        st = ExpokitStats()
+        check(lib().gbprop_expokit_advance(self._h, ptr(psi_dev), int(len(s)), ptr(s), dt.real, dt.imag,
+                                           float(tol), float(anorm), C.byref(st)))
+        return st
 
     def autotune(self, variant=-1):
         """Time the band kernel's tile shapes and keep the fastest (variant < 0), or select

@@ -13,7 +13,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cfloat>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -104,6 +106,8 @@ struct gbprop_ctx {
     std::vector<void*> allocs;
 
     cudaGraphExec_t graph = nullptr;      // one step on x (independent of the caller's buffers)
+    cudaGraphExec_t graph_arnoldi = nullptr;   // Expokit: the Arnoldi part alone (m+1 vectors)
+    long long arnoldi_launches = 0;
     long long graph_launches = 0;
     int band_variant = 1;             // tile shape of the band kernel (autotuner)
     int expm_max_cluster = 16;        // 1 when the handle is advanced inside a batch
@@ -112,6 +116,7 @@ struct gbprop_ctx {
 
     ~gbprop_ctx() {
         if (graph) cudaGraphExecDestroy(graph);
+        if (graph_arnoldi) cudaGraphExecDestroy(graph_arnoldi);
         for (void* p : allocs) cudaFree(p);
         if (ev_in) cudaEventDestroy(ev_in);
         if (ev_out) cudaEventDestroy(ev_out);
@@ -578,8 +583,10 @@ gbprop_status enqueue_leave(gbprop_ctx* h, void* psi, cudaStream_t s) {
     return GBPROP_OK;
 }
 
-// Enqueue one AdvanceStep on x (PamPropagator.py:50-57 around pamp.h:613-669).
-gbprop_status enqueue_step(gbprop_ctx* h) {
+// The Arnoldi part of a step on x (pamp.h:271-400): beta0 = ||x||, m basis vectors, the
+// Hessenberg matrix.  dorth: re-orthogonalisation passes (pamp.h:353-400); brk_tol: the
+// happy-breakdown threshold.
+gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
     cudaStream_t s = h->stream;
     const int kp = h->kprec();
     const int m = h->m;
@@ -587,7 +594,7 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
     char* V = (char*)h->d_V;
     const size_t vbytes = (size_t)N * h->kelem();
     GB_LAUNCH(launch_step_begin(h->d_ctrl, h->d_H, m, s));
-    const bool fused = h->cgs_grid > 0 && !h->double_orth && h->expm_max_cluster > 1;
+    const bool fused = h->cgs_grid > 0 && !dorth && h->expm_max_cluster > 1;
     if (fused) GB_CUDA(cudaMemsetAsync(h->d_gridbar, 0, 2 * sizeof(unsigned), s));
     // beta0 = ||x||
     GB_LAUNCH(launch_norm(0, h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
@@ -610,11 +617,11 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
             continue;
         }
         GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0,
-                                 h->double_orth, s));
-        if (J < m - 1 || h->double_orth)
+                                 dorth, s));
+        if (J < m - 1 || dorth)
             GB_LAUNCH(launch_cgs_update(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl,
-                                        h->double_orth ? 2 : 0, s));
-        if (h->double_orth) {
+                                        dorth ? 2 : 0, s));
+        if (dorth) {
             for (int pass = 0; pass < 3; ++pass) {
                 GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, 0,
                                          s));
@@ -622,8 +629,19 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
                                             s));
             }
         }
-        GB_LAUNCH(launch_arnoldi_finalize(h->d_ctrl, h->d_H, m, J, h->double_orth, s));
+        GB_LAUNCH(launch_arnoldi_finalize(h->d_ctrl, h->d_H, m, J, dorth, brk_tol, s));
     }
+    return GBPROP_OK;
+}
+
+// Enqueue one AdvanceStep on x (PamPropagator.py:50-57 around pamp.h:613-669).
+gbprop_status enqueue_step(gbprop_ctx* h) {
+    cudaStream_t s = h->stream;
+    const int kp = h->kprec();
+    const int m = h->m;
+    const long N = h->N;
+    char* V = (char*)h->d_V;
+    if (gbprop_status st = enqueue_arnoldi(h, h->double_orth, std::sqrt(DBL_EPSILON))) return st;   // pamp.h:79
     GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s));
     // x <- beta0 V exp(-i dt H) e1
     GB_LAUNCH(launch_combine(kp, V, h->d_v0, N, h->d_ctrl, h->d_x, s));
@@ -635,6 +653,10 @@ void drop_graph(gbprop_ctx* h) {
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
+    }
+    if (h->graph_arnoldi) {
+        cudaGraphExecDestroy(h->graph_arnoldi);
+        h->graph_arnoldi = nullptr;
     }
 }
 
@@ -1073,6 +1095,270 @@ gbprop_status gbprop_block_inner_product(int precision, const void* V, long n, i
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Expokit driver (ExpokitPropagator: adaptive Krylov sub-steps with local error control)
+// ---------------------------------------------------------------------------
+namespace {
+
+using cplx = std::complex<double>;
+
+// exp(t H) of an n x n complex matrix (row-major) by the diagonal Pade (6,6) approximant with
+// scaling and squaring, in the form of Expokit's zgpadm (Sidje 1998): s = max(0,
+// floor(log2 ||tH||_inf) + 2), Horner in (tH/2^s)^2 alternating the two polynomials, the odd
+// one times tH/2^s, E = I + 2 (Q - P)^-1 P (negated when s = 0 and the parity is odd), then
+// s squarings.  Returns false when the denominator is singular.
+bool expokit_pade(const std::vector<cplx>& H, int n, double t, std::vector<cplx>& E) {
+    const int p = 6;
+    double hn = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double r = 0.0;
+        for (int j = 0; j < n; ++j) r += std::abs(H[(size_t)i * n + j]);
+        hn = std::max(hn, r);
+    }
+    hn = std::fabs(t * hn);
+    if (hn == 0.0) {
+        E.assign((size_t)n * n, cplx(0.0));
+        for (int i = 0; i < n; ++i) E[(size_t)i * n + i] = 1.0;
+        return true;
+    }
+    const int ns = std::max(0, (int)(std::log(hn) / std::log(2.0)) + 2);
+    const double sc = t / std::ldexp(1.0, ns), sc2 = sc * sc;
+    double c[p + 1];
+    c[0] = 1.0;
+    for (int k = 1; k <= p; ++k) c[k] = c[k - 1] * (double)(p + 1 - k) / (double)(k * (2 * p + 1 - k));
+    auto mul = [n](const std::vector<cplx>& A, const std::vector<cplx>& B, std::vector<cplx>& C_, cplx alpha) {
+        C_.assign((size_t)n * n, cplx(0.0));
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < n; ++k) {
+                const cplx a = alpha * A[(size_t)i * n + k];
+                if (a == cplx(0.0)) continue;
+                for (int j = 0; j < n; ++j) C_[(size_t)i * n + j] += a * B[(size_t)k * n + j];
+            }
+    };
+    std::vector<cplx> H2, P((size_t)n * n, 0.0), Q((size_t)n * n, 0.0), T;
+    mul(H, H, H2, cplx(sc2));
+    for (int i = 0; i < n; ++i) {
+        P[(size_t)i * n + i] = c[p - 1];
+        Q[(size_t)i * n + i] = c[p];
+    }
+    int odd = 1;
+    for (int k = p - 1; k > 0; --k) {
+        mul(odd ? Q : P, H2, T, cplx(1.0));
+        for (int i = 0; i < n; ++i) T[(size_t)i * n + i] += c[k - 1];
+        (odd ? Q : P).swap(T);
+        odd = 1 - odd;
+    }
+    mul(odd ? Q : P, H, T, cplx(sc));
+    (odd ? Q : P).swap(T);
+    for (size_t k = 0; k < Q.size(); ++k) Q[k] -= P[k];
+    // Q X = P by LU with partial pivoting (largest |re| + |im|)
+    std::vector<int> piv(n);
+    for (int k = 0; k < n; ++k) {
+        int best = k;
+        double bv = -1.0;
+        for (int r = k; r < n; ++r) {
+            const cplx v = Q[(size_t)r * n + k];
+            const double a = std::fabs(v.real()) + std::fabs(v.imag());
+            if (a > bv) { bv = a; best = r; }
+        }
+        if (bv == 0.0) return false;
+        piv[k] = best;
+        if (best != k) {
+            for (int j = 0; j < n; ++j) std::swap(Q[(size_t)k * n + j], Q[(size_t)best * n + j]);
+            for (int j = 0; j < n; ++j) std::swap(P[(size_t)k * n + j], P[(size_t)best * n + j]);
+        }
+        const cplx inv = 1.0 / Q[(size_t)k * n + k];
+        for (int r = k + 1; r < n; ++r) {
+            const cplx f = Q[(size_t)r * n + k] * inv;
+            if (f == cplx(0.0)) continue;
+            for (int j = k; j < n; ++j) Q[(size_t)r * n + j] -= f * Q[(size_t)k * n + j];
+            for (int j = 0; j < n; ++j) P[(size_t)r * n + j] -= f * P[(size_t)k * n + j];
+        }
+    }
+    for (int r = n - 1; r >= 0; --r)
+        for (int j = 0; j < n; ++j) {
+            cplx a = P[(size_t)r * n + j];
+            for (int k = r + 1; k < n; ++k) a -= Q[(size_t)r * n + k] * P[(size_t)k * n + j];
+            P[(size_t)r * n + j] = a / Q[(size_t)r * n + r];
+        }
+    E.assign((size_t)n * n, cplx(0.0));
+    for (size_t k = 0; k < P.size(); ++k) E[k] = 2.0 * P[k];
+    for (int i = 0; i < n; ++i) E[(size_t)i * n + i] += 1.0;
+    if (ns == 0 && odd) {
+        for (cplx& v : E) v = -v;
+        return true;
+    }
+    for (int k = 0; k < ns; ++k) {
+        mul(E, E, T, cplx(1.0));
+        E.swap(T);
+    }
+    return true;
+}
+
+// Expokit's step-size rounding: two significant digits, rounded up (zgexpv).
+double expokit_round(double x) {
+    const int e = (int)std::lround(std::log10(x) - std::sqrt(0.1)) - 1;
+    const double p = std::pow(10.0, (double)e);
+    return std::trunc(x / p + 0.55) * p;
+}
+
+gbprop_status ensure_arnoldi_graph(gbprop_ctx* h) {
+    if (h->graph_arnoldi) return GBPROP_OK;
+    cudaGraph_t g = nullptr;
+    GB_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = launch_count();
+    gbprop_status st = enqueue_arnoldi(h, 1, 1e-7);      // re-orthogonalised; zgexpv break_tol
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (st) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    h->arnoldi_launches = launch_count() - before;
+    count_launch((int)-h->arnoldi_launches);
+    e = cudaGraphInstantiate(&h->graph_arnoldi, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return GBPROP_OK;
+}
+
+}  // namespace
+
+extern "C" gbprop_status gbprop_expokit_advance(gbprop_handle h, void* psi, int nsteps, const double* scalings,
+                                                double dt_re, double dt_im, double tol, double anorm,
+                                                gbprop_expokit_stats* stats) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!psi) return fail(GBPROP_EINVAL, "null wavefunction");
+    if (nsteps < 0) return fail(GBPROP_EINVAL, "negative step count");
+    if (!scalings && nsteps > 0) return fail(GBPROP_EINVAL, "null scaling schedule");
+    const int m = h->m - 1;
+    if (m < 2) return fail(GBPROP_EINVAL, "Expokit needs a handle with krylov_basis_size >= 3 (m + 1 vectors)");
+    if (!(anorm > 0.0)) return fail(GBPROP_EINVAL, "krylov_norm must be positive");
+    gbprop_expokit_stats acc = {0, 0, 0, 0.0, 1.0, 0.0};
+    if (nsteps == 0) {
+        if (stats) *stats = acc;
+        return GBPROP_OK;
+    }
+    const double eps = DBL_EPSILON;
+    if (tol <= eps) tol = std::sqrt(eps);
+    const double rndoff = eps * anorm;
+    const double t_out = std::sqrt(dt_re * dt_re + dt_im * dt_im);
+    const bool imag_time = std::fabs(dt_im) > 1e-10;     // expokitpropagator.cpp:61-66
+    // the callback applies -i A (real time) or -A (imaginary time) (krylovcommon.h:61-70)
+    const cplx fac = imag_time ? cplx(-1.0, 0.0) : cplx(0.0, -1.0);
+    const int mh = m + 2, mv = m + 1;                    // augmented size; device Hessenberg is mv x mv
+    gbprop_status st;
+    GB_CUDA(h->begin());
+    if ((st = enqueue_enter(h, psi, h->stream))) return st;
+    if ((st = ensure_sched(h, 1))) return st;
+    if ((st = ensure_arnoldi_graph(h))) return st;
+    std::vector<double> Hd((size_t)2 * mv * mv);
+    std::vector<cplx> Ha, F, Hs;
+    Ctrl c;
+    double vnorm = -1.0;
+    for (int n = 0; n < nsteps; ++n) {
+        SchedEntry se = {scalings[n], dt_re, dt_im};
+        GB_CUDA(cudaMemcpyAsync(h->d_sched, &se, sizeof(se), cudaMemcpyHostToDevice, h->stream));
+        double t_now = 0.0, t_new = 0.0, xm = 1.0 / m;
+        bool first = true;
+        while (t_now < t_out) {
+            // Arnoldi from the current state (beta = ||w||, m + 1 vectors, Hessenberg)
+            GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), h->stream));
+            GB_CUDA(cudaGraphLaunch(h->graph_arnoldi, h->stream));
+            count_launch((int)h->arnoldi_launches);
+            GB_CUDA(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+            GB_CUDA(cudaMemcpyAsync(Hd.data(), h->d_H, Hd.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            GB_CUDA(cudaStreamSynchronize(h->stream));
+            if (c.nonfinite) return fail(GBPROP_ENONFINITE, "non-finite Krylov norm");
+            if (c.wait_timeout) return fail(GBPROP_ETIMEOUT, "a bounded device wait gave up");
+            const double beta = c.beta0;
+            if (vnorm < 0.0) vnorm = beta;
+            acc.hump = std::max(acc.hump, beta / vnorm);
+            if (first) {
+                // initial step size (zgexpv)
+                const double p2 = tol * std::pow((m + 1) / 2.72, m + 1) * std::sqrt((m + 1) * 6.28);
+                t_new = expokit_round(1.0 / anorm * std::pow(p2 / (4.0 * beta * anorm), xm));
+                first = false;
+            }
+            double t_step = std::min(t_out - t_now, t_new);
+            int k1 = 2, mb = m;
+            double avnorm = 0.0;
+            if (c.broken) {
+                k1 = 0;
+                mb = c.nbasis;
+                t_step = t_out - t_now;
+            } else {
+                avnorm = c.pre_norm;                     // ||A v_{m+1}|| before orthogonalisation
+            }
+            acc.matvecs += c.broken ? c.nbasis : mv;
+            // augmented (m+2) x (m+2) matrix for the operator fac*A on the basis built for A:
+            // fac * H_A (its Krylov approximation beta V exp(t fac H_A) e1 and the magnitudes of
+            // the error-estimate entries equal those of the Hessenberg zgexpv builds for fac*A,
+            // whose basis differs from V only by the phases fac^j); H(m+1, m) = 1
+            Ha.assign((size_t)mh * mh, cplx(0.0));
+            for (int J = 0; J < mb; ++J)
+                for (int k = 0; k <= std::min(J + 1, mb); ++k) {
+                    if (k >= mv) continue;
+                    const cplx v(Hd[2 * ((size_t)k * mv + J)], Hd[2 * ((size_t)k * mv + J) + 1]);
+                    Ha[(size_t)k * mh + J] = fac * v;
+                }
+            if (k1 != 0) Ha[(size_t)(m + 1) * mh + m] = 1.0;
+            int ireject = 0;
+            double err_loc = 0.0;
+            int mx = mb + k1;
+            for (;;) {
+                mx = mb + k1;
+                Hs.assign((size_t)mx * mx, cplx(0.0));
+                for (int i = 0; i < mx; ++i)
+                    for (int j = 0; j < mx; ++j) Hs[(size_t)i * mx + j] = Ha[(size_t)i * mh + j];
+                if (!expokit_pade(Hs, mx, t_step, F)) return fail(GBPROP_ELU, "singular Pade denominator (Expokit)");
+                if (k1 == 0) {
+                    err_loc = tol;
+                    break;
+                }
+                const double p1 = std::abs(F[(size_t)m * mx]) * beta;
+                const double p2 = std::abs(F[(size_t)(m + 1) * mx]) * beta * avnorm;
+                if (p1 > 10.0 * p2) {
+                    err_loc = p2;
+                    xm = 1.0 / m;
+                } else if (p1 > p2) {
+                    err_loc = p1 * p2 / (p1 - p2);
+                    xm = 1.0 / m;
+                } else {
+                    err_loc = p1;
+                    xm = 1.0 / (m - 1);
+                }
+                if (err_loc <= 1.2 * t_step * tol) break;
+                t_step = expokit_round(0.9 * t_step * std::pow(t_step * tol / err_loc, xm));
+                ++acc.rejections;
+                if (++ireject > 100) return fail(GBPROP_EBREAKDOWN, "Expokit: the requested tolerance is too high");
+            }
+            // w = beta V exp(t_step H) e1 over mx = mb + max(0, k1 - 1) vectors
+            mx = mb + std::max(0, k1 - 1);
+            const int ld = mb + k1;
+            std::vector<double> y((size_t)2 * mx);
+            for (int k = 0; k < mx; ++k) {
+                y[2 * k] = F[(size_t)k * ld].real();
+                y[2 * k + 1] = F[(size_t)k * ld].imag();
+            }
+            GB_CUDA(cudaMemcpyAsync(h->d_ctrl->y, y.data(), y.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                    h->stream));
+            GB_CUDA(cudaMemcpyAsync(&h->d_ctrl->nbasis, &mx, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+            GB_CUDA(cudaMemsetAsync(&h->d_ctrl->broken, 0, sizeof(int), h->stream));
+            GB_LAUNCH(launch_combine(h->kprec(), h->d_V, h->d_v0, h->N, h->d_ctrl, h->d_x, h->stream));
+            t_now += t_step;
+            t_new = expokit_round(0.9 * t_step * std::pow(t_step * tol / err_loc, xm));
+            acc.error += std::max(err_loc, rndoff);
+            acc.last_step = t_step;
+            ++acc.substeps;
+        }
+    }
+    if ((st = enqueue_leave(h, psi, h->stream))) return st;
+    GB_CUDA(h->end());
+    if (stats) *stats = acc;
+    return GBPROP_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Batches: many independent problems advanced together.  The step sequences

@@ -126,7 +126,8 @@ struct Ctrl {
     double beta0;           // ||U psi|| at the start of the step
     double beta;            // current residual norm
     double inv_beta;        // 1 / beta (the reference scales by the reciprocal)
-    double orig_norm;       // ||w|| before Gram-Schmidt (re-orthogonalisation rule)
+    double orig_norm;       // ||w|| before Gram-Schmidt (re-orthogonalisation rule; updated per pass)
+    double pre_norm;        // ||w|| of the operator output, before any Gram-Schmidt pass
     double resid_norm;      // ||w|| after Gram-Schmidt
     double err_est;         // |y[m-1]|^2
     double h[2 * kMaxBasis];
@@ -186,7 +187,10 @@ cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const vo
                                double* partials, unsigned* counter, cudaStream_t s);
 cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, long n, int nv, void* w, double* partials,
                               unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
-cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, cudaStream_t s);
+// brk_tol: happy-breakdown threshold on the new basis norm (pAMP: sqrt(eps), pamp.h:79;
+// Expokit: 1e-7).
+cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol,
+                                    cudaStream_t s);
 // One Arnoldi step's Gram-Schmidt (dot, update, norm, Hessenberg column, breakdown) as a
 // single cooperative kernel of `grid` co-resident CTAs (gbprop_cgs.cu).  part: at least
 // arnoldi_cgs_part_doubles(grid) doubles; bar: two words, zero before the first launch.

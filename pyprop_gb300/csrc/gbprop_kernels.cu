@@ -617,7 +617,10 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict
     if (ctrl) {
         double* dst = mode ? ctrl->h3 : ctrl->h;
         for (int q = tid; q < 2 * nv; q += kDotThreads) dst[q] = tot[q];
-        if (tid == 0 && want_norm && mode == 0) ctrl->orig_norm = sqrt(tot[2 * nv]);
+        if (tid == 0 && want_norm && mode == 0) {
+            ctrl->orig_norm = sqrt(tot[2 * nv]);
+            ctrl->pre_norm = ctrl->orig_norm;
+        }
     } else {
         for (int q = tid; q < 2 * nv; q += kDotThreads) hout[q] = tot[q];
         if (tid == 0 && want_norm) hout[2 * nv] = tot[2 * nv];
@@ -805,7 +808,7 @@ cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, long n
 
 // Writes Hessenberg column J, the next beta and the happy-breakdown decision
 // (pamp.h:305-315, 345).
-__global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth) {
+__global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol) {
     if (ctrl->broken) return;
     const int nv = J + 1;
     for (int k = threadIdx.x; k < nv; k += blockDim.x) {
@@ -820,9 +823,8 @@ __global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int doub
         if (double_orth && ctrl->ro_go && ctrl->ro_count >= 3) ctrl->orthogonalization_count++;
         if (J + 1 < m) {
             const double beta = ctrl->resid_norm;
-            const double tol = sqrt(DBL_EPSILON);   // pamp.h:79
             if (!isfinite(beta)) ctrl->nonfinite = 1;
-            if (fabs(beta) < tol) {
+            if (fabs(beta) < brk_tol) {
                 ctrl->broken = 1;
                 ctrl->breakdown_count++;
             } else {
@@ -835,9 +837,10 @@ __global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int doub
     }
 }
 
-cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, cudaStream_t s) {
+cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol,
+                                    cudaStream_t s) {
     count_launch();
-    k_arnoldi_finalize<<<1, 64, 0, s>>>(ctrl, H, m, J, double_orth);
+    k_arnoldi_finalize<<<1, 64, 0, s>>>(ctrl, H, m, J, double_orth, brk_tol);
     return cudaGetLastError();
 }
 

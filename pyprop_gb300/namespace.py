@@ -47,6 +47,7 @@ def eval_namespace():
     ns["PotentialType"] = PotentialType
     ns["InitialConditionType"] = problem.InitialConditionType
     ns["PamPropagator"] = propagator.PamPropagator
+    ns["ExpokitPropagator"] = propagator.ExpokitPropagator
     ns["BasisPropagator"] = propagator.BasisPropagator
     ns["LaserFunctionVelocity"] = potentials.LaserFunctionVelocity
     ns["LaserFunctionSimpleLength"] = potentials.LaserFunctionSimpleLength

@@ -230,3 +230,65 @@ class PamPropagator(PropagatorBase):
 
     def Handle(self):
         return self._handle
+
+
+class ExpokitPropagator(PropagatorBase):
+    """Expokit Krylov propagator (pyprop/propagator/KrylovPropagator.py:2-58): the same
+    balanced-overlap matvec inside zgexpv's adaptive sub-stepping with local error control
+    (core/krylov/expokit/expokitpropagator.cpp:18-103).  Keys: krylov_basis_size,
+    krylov_tolerance, krylov_norm (an estimate of the operator's norm, used for the first
+    sub-step size)."""
+
+    def __init__(self, psi):
+        PropagatorBase.__init__(self, psi)
+        self.Rank = psi.GetRank()
+        self.BasisSize = 20
+        self.Tolerance = 0.0
+        self.MatrixNorm = 1.0
+        self.Precision = _native.FP64
+        self.Autotune = True
+        self._handle = None
+        self.Statistics = None
+
+    def ApplyConfig(self, config):
+        PropagatorBase.ApplyConfig(self, config)
+        propagatorType = config.Propagation.base_propagator
+        self.BasePropagator = propagatorType(self.psi)
+        config.Apply(self.BasePropagator)
+
+    def ApplyConfigSection(self, sec):
+        PropagatorBase.ApplyConfigSection(self, sec)
+        sec.Apply(self.BasePropagator)
+        self.BasisSize = int(sec.krylov_basis_size)
+        self.Tolerance = float(sec.krylov_tolerance)
+        self.MatrixNorm = float(sec.krylov_norm)
+        if hasattr(sec, "krylov_precision"):
+            self.Precision = precision_of(sec.krylov_precision)
+        if hasattr(sec, "krylov_autotune"):
+            self.Autotune = bool(sec.krylov_autotune)
+
+    def SetupStep(self, dt):
+        self.BasePropagator.SetupStep(dt)
+        _require_device(self.psi)
+        # m + 1 basis vectors: zgexpv's extra operator application A v_{m+1}
+        self._handle = build_handle(self.psi, self.BasePropagator.PotentialList, self.Precision,
+                                    self.BasisSize + 1, 0, True)
+        if self.Autotune:
+            self._handle.autotune()
+        self.BasePropagator.AttachHandle(self._handle)
+        self.TempPsi = self.psi.CopyDeep()
+
+    def AdvanceStep(self, t, dt):
+        self.AdvanceSteps([t], dt)
+
+    def AdvanceSteps(self, times, dt):
+        if self._handle is None:
+            raise RuntimeError("SetupStep must be called before AdvanceStep")
+        scal = np.array([self.BasePropagator._scaling(t) for t in times], dtype=np.float64)
+        self.Statistics = self._handle.expokit_advance(self.psi.data, scal, dt, self.Tolerance, self.MatrixNorm)
+
+    def MultiplyHamiltonian(self, srcPsi, destPsi, t, dt):
+        self.BasePropagator.MultiplyHamiltonian(srcPsi, destPsi, t, dt)
+
+    def Handle(self):
+        return self._handle
