@@ -506,12 +506,16 @@ void set_inv_chunks(gbprop_ctx* h, bool wide) {
             for (int q0 = 0; q0 < n; q0 += chunk) mx = std::max(mx, inv_smem_bytes(n, q0, chunk, P, w, kd, stage, 1));
             return mx;
         };
-        auto cost = [&](int chunk) {
+        // cost ~ (waves of resident CTAs) x (elements one CTA processes over all passes); CTAs
+        // that fit two per SM count as half a wave each (their latency-bound phases overlap)
+        auto cost = [&](int chunk, int stage) {
             const int nch = (n + chunk - 1) / chunk;
             long work = 0;
-            for (int k = 1; k <= P; ++k) work += std::min(n, chunk + (P - k) * (w + kd) + w);
-            const long waves = ((long)h->nl * nch + sms - 1) / sms;
-            return waves * (work + chunk);
+            for (int k = 0; k <= P; ++k) work += std::min(n, chunk + (P - k) * (w + kd) + w);
+            const size_t sm = smem_of(chunk, stage) + 1024;
+            const int per_sm = std::max(1, std::min(2, (int)((size_t)228 * 1024 / sm)));
+            const long waves = ((long)h->nl * nch + (long)sms * per_sm - 1) / ((long)sms * per_sm);
+            return waves * work * 2 / per_sm;
         };
         int best = -1, best_stage = 0;
         long best_cost = 0;
@@ -520,7 +524,7 @@ void set_inv_chunks(gbprop_ctx* h, bool wide) {
                 const int chunk = chunk_of(nch);
                 if (nch > 1 && chunk < 32) break;
                 if (smem_of(chunk, stage) > (size_t)220 * 1024) continue;
-                const long c = cost(chunk);
+                const long c = cost(chunk, stage);
                 if (best < 0 || (wide ? c < best_cost : false)) {
                     best = chunk;
                     best_cost = c;

@@ -42,8 +42,8 @@ template <typename T> struct SolveTab {
 //   m  (j*npad + q)  FP32, zero where q + j >= n;  npad = n rounded up to 4
 //   u  (d*npad + q)  FP64, zero where q + d >= n
 // Each CTA owns `chunk` radial elements (a multiple of 4) of one row and recomputes the
-// halo its refinement passes need; stage = 1 copies the chunk's slices of m and u into
-// shared memory with bulk asynchronous copies (16-byte aligned: q0, npad multiples of 4).
+// halo its refinement passes need; stage = 1 copies the chunk's slice of m into shared memory
+// with bulk asynchronous copies (16-byte aligned: q0, npad multiples of 4).
 struct InvTab {
     int n, kd, w, npad;
     int chunk, nchunks;
@@ -66,8 +66,9 @@ __host__ __device__ inline void inv_region(int n, int q0, int chunk, int P, int 
     *RB = rb < left ? rb : left;
 }
 
-// Shared-memory bytes of that CTA: b | x, r (FP64, refined solve only) | M slice (staged) |
-// U~ slice (staged, refined solve only) | r32.
+// Shared-memory bytes of that CTA: b | x, r (FP64, refined solve only) | M slice (staged; read
+// three times) | r32 | x0 (FP32 first iterate, refined solve only).  U~ is read once per
+// residual pass and comes through L2.
 __host__ __device__ inline size_t inv_smem_bytes(int n, int q0, int chunk, int P, int w, int kd, int stage, int r64) {
     int cl, R0, RB;
     inv_region(n, q0, chunk, P, w, kd, &cl, &R0, &RB);
@@ -75,8 +76,8 @@ __host__ __device__ inline size_t inv_smem_bytes(int n, int q0, int chunk, int P
     size_t b = (size_t)RB * 16;
     if (r64) b += (size_t)R0 * 16 + (size_t)RB * 16;
     if (stage) b += (size_t)(w + 1) * R0p * 4;
-    if (stage && r64) b += (size_t)(kd + 1) * R0p * 8;
     b += (size_t)(R0 + w) * 8;
+    if (r64) b += (size_t)R0 * 8;
     return b;
 }
 

@@ -449,12 +449,14 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
     if (R64) sp += (size_t)R0 * 16 + (size_t)RB * 16;
     float* Ms = reinterpret_cast<float*>(sp);
     if (STAGE) sp += (size_t)(w + 1) * R0p * 4;
-    double* Us = reinterpret_cast<double*>(sp);
-    if (STAGE && R64) sp += (size_t)(KD + 1) * R0p * 8;
     float2* r32 = reinterpret_cast<float2*>(sp);
+    sp += (size_t)(R0 + w) * 8;
+    float2* x0f = reinterpret_cast<float2*>(sp);     // FP32 first iterate (exact in FP32)
 
     const float* Mg = tab.m + q0;
     const double* Ug = tab.u + q0;
+    const float* Uhg = tab.uh + q0;
+    const float* Ulg = tab.ul + q0;
     if (STAGE) {
         // one thread arms the barrier with the byte count and issues one bulk copy per
         // diagonal (rows of R0p elements: sizes and addresses are multiples of 16 bytes)
@@ -464,19 +466,19 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
         }
         __syncthreads();                               // barrier initialised before anyone polls it
         if (tid == 0) {
-            const unsigned mrow = (unsigned)R0p * 4, urow = (unsigned)R0p * 8;
-            const unsigned bytes = (unsigned)(w + 1) * mrow + (R64 ? (unsigned)(KD + 1) * urow : 0u);
+            const unsigned mrow = (unsigned)R0p * 4;
+            const unsigned bytes = (unsigned)(w + 1) * mrow;
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                          :: "r"(smem_u32(&s_bar)), "r"(bytes) : "memory");
             for (int j = 0; j <= w; ++j) bulk_g2s(Ms + (size_t)j * R0p, Mg + (size_t)j * tab.npad, mrow, &s_bar);
-            if (R64)
-                for (int d = 0; d <= KD; ++d) bulk_g2s(Us + (size_t)d * R0p, Ug + (size_t)d * tab.npad, urow, &s_bar);
         }
     }
     const float* mbase = STAGE ? Ms : Mg;
     const size_t mstride = STAGE ? (size_t)R0p : (size_t)tab.npad;
-    const double* ubase = STAGE ? Us : Ug;
-    const size_t ustride = STAGE ? (size_t)R0p : (size_t)tab.npad;
+    const double* ubase = Ug;
+    const float* uhb = Uhg;
+    const float* ulb = Ulg;
+    const size_t ustride = (size_t)tab.npad;
     const double sc = scale_mode ? ctrl->inv_beta : 1.0;
     const size_t base = (size_t)l * n;
 
@@ -497,9 +499,51 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
             if (STAGE) mbar_wait0(&s_bar);
             return;
         }
+        bool x0_exact = false;                     // x after pass 0 is the FP32 vector x0f
         for (int k = 0; k <= P; ++k) {
             const int Rk = min(n - q0, cl + (P - k) * (w + KD));
             const int Rr = min(n - q0, Rk + w);
+            if (k == 1 && P >= 2 && x0_exact) {
+                // first refinement: r = b - U~ x0 with x0 exact in FP32, formed with FP32 pairs
+                // (U~ = uh + ul, b = bh + bl; error-free products and sums).  Its relative error
+                // (~2^-48 |b| / |r|) is far below what this pass needs; the last pass uses an FP64
+                // residual.  No scaling: |b| has an FP32-safe exponent (checked at pass 0).
+                for (int q = tid; q < Rk + w; q += kInvThreads) {
+                    float2 v = make_float2(0.f, 0.f);
+                    if (q < Rr) {
+                        float hr = 0.f, lr = 0.f, hi_ = 0.f, li = 0.f;
+#pragma unroll
+                        for (int d = 0; d <= KD; ++d) {
+                            if (q + d < n - q0) {
+                                const float uh = __ldg(uhb + (size_t)d * ustride + q);
+                                const float ul = __ldg(ulb + (size_t)d * ustride + q);
+                                const float2 xv = x0f[q + d];
+                                acc_prod(hr, lr, uh, ul, xv.x);
+                                acc_prod(hi_, li, uh, ul, xv.y);
+                            }
+                        }
+                        const double2 b = bq[q];
+                        const float bhx = (float)b.x, bhy = (float)b.y;
+                        const float blx = (float)(b.x - (double)bhx), bly = (float)(b.y - (double)bhy);
+                        float s_, e_;
+                        two_sum(bhx, -hr, s_, e_);
+                        v.x = __fadd_rn(s_, __fadd_rn(e_, __fsub_rn(blx, lr)));
+                        two_sum(bhy, -hi_, s_, e_);
+                        v.y = __fadd_rn(s_, __fadd_rn(e_, __fsub_rn(bly, li)));
+                    }
+                    r32[q] = v;
+                }
+                __syncthreads();
+                for (int q = tid; q < Rk; q += kInvThreads) {
+                    const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
+                    double2 x = xq[q];
+                    x.x += (double)f.x;
+                    x.y += (double)f.y;
+                    xq[q] = x;
+                }
+                __syncthreads();
+                continue;
+            }
             // residual r = b - U~ x (FP64, two FMA chains per component) and the max of
             // its high words (monotone in |r|)
             unsigned hmax = 0;
@@ -510,7 +554,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
 #pragma unroll
                     for (int d = 0; d <= KD; ++d) {
                         if (q + d < n - q0) {
-                            const double u = ubase[(size_t)d * ustride + q];
+                            const double u = __ldg(ubase + (size_t)d * ustride + q);
                             const double2 xv = xq[q + d];
                             if (d & 1) { ar = fma(-u, xv.x, ar); ai = fma(-u, xv.y, ai); }
                             else { r.x = fma(-u, xv.x, r.x); r.y = fma(-u, xv.y, r.y); }
@@ -550,7 +594,9 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                 if (scaled) { x.x = fma((double)f.x, sup, x.x); x.y = fma((double)f.y, sup, x.y); }
                 else { x.x += (double)f.x; x.y += (double)f.y; }
                 xq[q] = x;
+                if (k == 0) x0f[q] = f;                  // x0 = f exactly when unscaled
             }
+            if (k == 0) x0_exact = !scaled && e > -60 && e < 60;   // the FP32-pair residual stays normal
             __syncthreads();
         }
         for (int q = tid; q < cl; q += kInvThreads) {
