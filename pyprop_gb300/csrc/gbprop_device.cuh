@@ -57,6 +57,32 @@ __device__ __forceinline__ void acc_scaled(float& hi, float& lo, float ch, float
     lo = __fadd_rn(lo, __fadd_rn(t, __fadd_rn(pe, __fmaf_rn(ch, sl, __fmul_rn(cl, sh)))));
 }
 
+// Programmatic dependent launch: a kernel launched with launch_pdl is scheduled as its
+// predecessor's CTAs retire (no explicit early trigger: CTAs of the next kernel waiting on
+// SMs slowed the solve measurably), hiding the launch gap between stream-launched kernels;
+// inside a captured graph the gap is already small.  The kernel must execute pdl_wait()
+// before it reads anything the predecessor wrote and before any early return (so that
+// completion stays transitive along a chain of such kernels).  Without the launch
+// attribute pdl_wait is a no-op.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+bool pdl_enabled();                         // GBPROP_PDL=0 disables the attribute
+
+template <typename K, typename... Args>
+inline cudaError_t launch_pdl(K kern, dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // Raise a kernel's dynamic shared-memory limit to the device's opt-in maximum, once per
 // kernel.  The limit then does not depend on which launch set it last, so graph nodes of
 // one kernel with different shared-memory sizes all stay valid, also when a tool replays

@@ -14,6 +14,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cfloat>
 #include <cmath>
 
@@ -166,6 +167,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
     constexpr int W = 2 * KB + 1;
     constexpr int TILE = THREADS * PER;
     __shared__ C sx[TILE + 2 * KB];
+    pdl_wait();
     if (check_broken && ctrl->broken) return;
     const int l = blockIdx.y, i0 = blockIdx.x * TILE, tid = threadIdx.x;
     const int nr = op.nr;
@@ -277,6 +279,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply_l1(BandOp<T> op, const c
                                                            int check_broken) {
     using C = cx<T>;
     constexpr int W = 2 * KB + 1;
+    pdl_wait();
     if (check_broken && ctrl->broken) return;
     const int l = blockIdx.y, nr = op.nr;
     const int i = blockIdx.x * THREADS + threadIdx.x;
@@ -349,13 +352,14 @@ static void band_apply_v(const BandOp<T>& op, const void* x, void* y, const Sche
     if constexpr (V >= 4) {
         constexpr int TH = band_threads(V);
         dim3 grid((op.nr + TH - 1) / TH, op.nl);
-        k_band_apply_l1<T, KB, TH><<<grid, TH, 0, s>>>(op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl, scaling,
-                                                       check_broken);
+        launch_pdl(k_band_apply_l1<T, KB, TH>, grid, dim3(TH), 0, s, op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl,
+                   scaling, check_broken);
         return;
     }
     constexpr int TH = band_threads(V), PE = band_per(V);
     dim3 grid((op.nr + TH * PE - 1) / (TH * PE), op.nl);
-    k_band_apply<T, KB, TH, PE><<<grid, TH, 0, s>>>(op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl, scaling, check_broken);
+    launch_pdl(k_band_apply<T, KB, TH, PE>, grid, dim3(TH), 0, s, op, (const cx<T>*)x, (cx<T>*)y, sched, ctrl, scaling,
+               check_broken);
 }
 
 template <typename T, int KB>
@@ -441,6 +445,14 @@ constexpr int kRedThreads = 512;
 constexpr int kPStride = 2 * kMaxBasis + 4;   // doubles of partials per block
 
 int grid_reduce_blocks() { return 152; }
+
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("GBPROP_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
 
 // doubles of reduction scratch every launcher may use (update: up to 4*152 blocks of
 // kPStride; dot: 2 values per (value, chunk) with at most ~304 + values chunks)

@@ -433,7 +433,6 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ unsigned s_red[kInvThreads / 32];
     __shared__ __align__(8) unsigned long long s_bar;
-    if (check_broken && ctrl->broken) return;
     const int n = tab.n, w = tab.w, P = R64 ? tab.refine : 0;
     const int l = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int q0 = blockIdx.x * tab.chunk;
@@ -472,6 +471,13 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                          :: "r"(smem_u32(&s_bar)), "r"(bytes) : "memory");
             for (int j = 0; j <= w; ++j) bulk_g2s(Ms + (size_t)j * R0p, Mg + (size_t)j * tab.npad, mrow, &s_bar);
         }
+    }
+    // the band of M is constant and is staged before the wait; everything below reads what
+    // earlier kernels wrote
+    pdl_wait();
+    if (check_broken && ctrl->broken) {
+        if (STAGE) mbar_wait0(&s_bar);             // copies in flight land before exit
+        return;
     }
     const float* mbase = STAGE ? Ms : Mg;
     const size_t mstride = STAGE ? (size_t)R0p : (size_t)tab.npad;
@@ -622,7 +628,6 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
                                                              int check_broken) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long s_bar;
-    if (check_broken && ctrl->broken) return;
     const int n = tab.n, w = tab.w;
     const int l = blockIdx.y, tid = threadIdx.x;
     const int q0 = blockIdx.x * tab.chunk;
@@ -659,6 +664,11 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
                 bulk_g2s(Ul + (size_t)d * R0p, Ulg + (size_t)d * tab.npad, row, &s_bar);
             }
         }
+    }
+    pdl_wait();
+    if (check_broken && ctrl->broken) {
+        if (STAGE) mbar_wait0(&s_bar);
+        return;
     }
     const float* mbase = STAGE ? Ms : Mg;
     const size_t mstride = STAGE ? (size_t)R0p : (size_t)tab.npad;
@@ -743,9 +753,9 @@ static cudaError_t solve_mixed_launch(const InvTab& tab, int nrows, const void* 
             cudaError_t ea = allow_max_smem(kern);                                                               \
             if (ea != cudaSuccess) return ea;                                                                    \
         }                                                                                                        \
-        kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (float2*)out, (TV_*)vstore, ctrl, dir, scale_mode,   \
-                                       check_broken);                                                            \
-        return cudaGetLastError();                                                                               \
+        cudaError_t el = launch_pdl(kern, grid, block, smem, s, tab, (const TI_*)in, (float2*)out, (TV_*)vstore,  \
+                                    ctrl, dir, scale_mode, check_broken);                                        \
+        return el != cudaSuccess ? el : cudaGetLastError();                                                      \
     }
     // in: the FP64 first vector (with its FP64 copy stored) or a complex64 vector
     if (in_prec == 0 && v_prec == 0) GB_MIX_CASE(double2, double2)
@@ -770,9 +780,9 @@ static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in
             cudaError_t ea = allow_max_smem(kern);                                                               \
             if (ea != cudaSuccess) return ea;                                                                    \
         }                                                                                                        \
-        kern<<<grid, block, smem, s>>>(tab, (const TI_*)in, (TO_*)out, (TV_*)vstore, ctrl, dir, scale_mode,      \
-                                       check_broken);                                                            \
-        return cudaGetLastError();                                                                               \
+        cudaError_t el = launch_pdl(kern, grid, block, smem, s, tab, (const TI_*)in, (TO_*)out, (TV_*)vstore,     \
+                                    ctrl, dir, scale_mode, check_broken);                                        \
+        return el != cudaSuccess ? el : cudaGetLastError();                                                      \
     }
     // combinations the runtime uses: refined solves store double2 (or nothing)
     const int key = in_prec * 4 + out_prec * 2 + v_prec;
