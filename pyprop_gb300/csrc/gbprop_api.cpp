@@ -99,6 +99,7 @@ struct gbprop_ctx {
     void* d_y = nullptr;              // N, Krylov precision (H U^-1 v)
     double2* d_x = nullptr;           // N, complex128 (U psi, V y)
     double2* d_v0 = nullptr;          // N, complex128 first basis vector of a complex64 basis
+    float4* d_v0s = nullptr;          // N, the same split into FP32 pairs (re_hi, im_hi, re_lo, im_lo)
     int cgs_grid = 0;                 // > 0: Gram-Schmidt as one cooperative kernel of this many CTAs
     int cgs_cache = 0;                // its V chunk cached in shared memory
     double* d_cgs_part = nullptr;     // its partial sums
@@ -543,10 +544,10 @@ void set_inv_chunks(gbprop_ctx* h, bool wide) {
 // Triangular solve of the Krylov precision: FP64-accurate (FP32 solve + FP64 refinement)
 // for the FP64 path, plain complex64 for the mixed path's basis.
 cudaError_t ksolve(gbprop_ctx* h, int dir, const void* in, int in_prec, void* out, int out_prec, void* vstore,
-                   int v_prec, int scale_mode, int check_broken) {
+                   int v_prec, int scale_mode, int check_broken, float4* v0s = nullptr) {
     if (h->inv_ok)
         return launch_solve_inv(h->inv[dir], h->nl, h->prec == GBPROP_FP64 ? 1 : 0, in, in_prec, out, out_prec,
-                                vstore, v_prec, h->d_ctrl, dir, scale_mode, check_broken, h->stream);
+                                vstore, v_prec, h->d_ctrl, dir, scale_mode, check_broken, h->stream, v0s);
     if (h->prec == GBPROP_FP64)
         return launch_solve_ir(&h->t32.tab[dir], h->d_ud_phys, h->nl, in, in_prec, out, out_prec, vstore, v_prec,
                                h->d_ctrl, scale_mode, check_broken, h->stream);
@@ -598,7 +599,8 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
     char* V = (char*)h->d_V;
     const size_t vbytes = (size_t)N * h->kelem();
     GB_LAUNCH(launch_step_begin(h->d_ctrl, h->d_H, m, s));
-    const bool fused = h->cgs_grid > 0 && !dorth && h->expm_max_cluster > 1;
+    // the complex64 form reads the split first vector, which only the inverse-band solve writes
+    const bool fused = h->cgs_grid > 0 && !dorth && h->expm_max_cluster > 1 && (h->prec == GBPROP_FP64 || h->inv_ok);
     if (fused) GB_CUDA(cudaMemsetAsync(h->d_gridbar, 0, 2 * sizeof(unsigned), s));
     // beta0 = ||x||
     GB_LAUNCH(launch_norm(0, h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
@@ -607,7 +609,7 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
         const int in_prec = J == 0 ? 0 : kp;
         // v_J = r / beta_J stored in V[J] (v_0 of a complex64 basis in FP64); s = U^-1 v_J
         if (J == 0 && h->d_v0)
-            GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, h->d_v0, 0, 1, 1));
+            GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, h->d_v0, 0, 1, 1, fused ? h->d_v0s : nullptr));
         else
             GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1));
         // y = sum_t c_t s_t A_t s
@@ -616,7 +618,7 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
         GB_LAUNCH(ksolve(h, 1, h->d_y, kp, h->d_r, kp, nullptr, kp, 0, 1));
         // classical Gram-Schmidt against v_0..v_J
         if (fused) {
-            GB_LAUNCH(launch_arnoldi_cgs(kp, V, h->d_v0, N, J, m, h->d_r, h->d_cgs_part, h->d_gridbar, h->d_ctrl,
+            GB_LAUNCH(launch_arnoldi_cgs(kp, V, h->d_v0s, N, J, m, h->d_r, h->d_cgs_part, h->d_gridbar, h->d_ctrl,
                                          h->d_H, J < m - 1, h->cgs_grid, h->cgs_cache, s));
             continue;
         }
@@ -868,6 +870,7 @@ gbprop_status gbprop_finalize(gbprop_handle h) {
     if ((st = h->dalloc(&h->d_y, (size_t)h->N * ke))) return st;
     if ((st = h->dalloc(&h->d_x, (size_t)h->N * sizeof(double2)))) return st;
     if (h->prec != GBPROP_FP64 && (st = h->dalloc(&h->d_v0, (size_t)h->N * sizeof(double2)))) return st;
+    if (h->prec != GBPROP_FP64 && (st = h->dalloc(&h->d_v0s, (size_t)h->N * sizeof(float4)))) return st;
     // cooperative Gram-Schmidt (single handles; GBPROP_CGS=separate keeps the three-kernel form)
     {
         const char* env = std::getenv("GBPROP_CGS");

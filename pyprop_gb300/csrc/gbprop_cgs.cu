@@ -60,14 +60,12 @@ __device__ __forceinline__ void acc_dot64(double& ar, double& ai, double vr, dou
     ai = fma(-vi, xr, ai);
 }
 
-template <typename T, bool CACHE>
-__global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const cx<T>* __restrict__ V,
-                                                              const double2* __restrict__ v0, long n, int J, int m,
-                                                              cx<T>* __restrict__ w, double* __restrict__ part,
+template <bool CACHE>
+__global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __restrict__ V, long n, int J, int m,
+                                                              double2* __restrict__ w, double* __restrict__ part,
                                                               unsigned* bar, Ctrl* ctrl, double* H, int update,
                                                               int chunk) {
-    using C = cx<T>;
-    constexpr bool kF32 = sizeof(T) < sizeof(double);
+    using C = double2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double hs[2 * (kMaxBasis + 1)];
     __shared__ double red[kFuseThreads / 32];
@@ -75,92 +73,46 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const cx<T>* __res
     const int nv = J + 1, G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long i0 = (long)b * chunk;
     const int cl = (int)max(0L, min((long)chunk, n - i0));
-    // shared memory: w chunk | first vector (FP64, complex64 basis with v0) | cached rows
+    // shared memory: w chunk | cached rows of V
     C* ws = reinterpret_cast<C*>(smem_raw);
-    double2* c0 = reinterpret_cast<double2*>(smem_raw + (((size_t)chunk * sizeof(C) + 15) & ~(size_t)15));
-    C* cache = reinterpret_cast<C*>(reinterpret_cast<unsigned char*>(c0) + (v0 ? (size_t)chunk * 16 : 0));
+    C* cache = reinterpret_cast<C*>(smem_raw + (((size_t)chunk * sizeof(C) + 15) & ~(size_t)15));
     for (int i = tid; i < cl; i += kFuseThreads) ws[i] = w[i0 + i];
     __syncthreads();
 
-    // ---- phase A: partial inner products, one warp per basis vector ------------------------
+    // ---- phase A: partial inner products, one warp per basis vector.  The FP64 pipe retires
+    // one warp instruction per 16 SM cycles and its dependent latency is about as long, so two
+    // accumulator pairs per warp keep it busy; every extra add is pipe time. ----------------
     for (int k = warp; k < nv; k += kFuseThreads / 32) {
         double ar = 0.0, ai = 0.0, br = 0.0, bi = 0.0;
-        if (v0 && k == 0) {
-            for (int i = lane; i < cl; i += 32) {
-                const double2 v = v0[i0 + i];
-                if (CACHE) c0[i] = v;
-                const C x = ws[i];
-                acc_dot64(ar, ai, v.x, v.y, (double)x.x, (double)x.y);
-            }
-        } else if (kF32) {
-            // complex64 operands: error-free FP32 products, compensated FP32 sums; four
-            // loads in flight per lane, two independent compensated chains
-            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f, sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
-            const C* vk = V + (size_t)k * n + i0;
-            int i = lane;
-            for (; i + 96 < cl; i += 128) {
-                C v[4];
+        const C* vk = V + (size_t)k * n + i0;
+        int i = lane;
+        for (; i + 96 < cl; i += 128) {
+            C v[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = vk[i + 32 * u];
+            for (int u = 0; u < 4; ++u) v[u] = vk[i + 32 * u];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    if (CACHE) cache[(size_t)k * chunk + i + 32 * u] = v[u];
-                    const C x = ws[i + 32 * u];
-                    if (u & 1) {
-                        acc_prod(sh, sl, (float)v[u].x, 0.f, (float)x.x);
-                        acc_prod(sh, sl, (float)v[u].y, 0.f, (float)x.y);
-                        acc_prod(th, tl, (float)v[u].x, 0.f, (float)x.y);
-                        acc_prod(th, tl, -(float)v[u].y, 0.f, (float)x.x);
-                    } else {
-                        acc_prod(rh, rl, (float)v[u].x, 0.f, (float)x.x);
-                        acc_prod(rh, rl, (float)v[u].y, 0.f, (float)x.y);
-                        acc_prod(ih, il, (float)v[u].x, 0.f, (float)x.y);
-                        acc_prod(ih, il, -(float)v[u].y, 0.f, (float)x.x);
-                    }
-                }
+            for (int u = 0; u < 4; ++u) {
+                if (CACHE) cache[(size_t)k * chunk + i + 32 * u] = v[u];
+                const C x = ws[i + 32 * u];
+                if (u & 1) acc_dot64(br, bi, v[u].x, v[u].y, x.x, x.y);
+                else acc_dot64(ar, ai, v[u].x, v[u].y, x.x, x.y);
             }
-            for (; i < cl; i += 32) {
-                const C v = vk[i];
-                if (CACHE) cache[(size_t)k * chunk + i] = v;
-                const C x = ws[i];
-                acc_prod(rh, rl, (float)v.x, 0.f, (float)x.x);
-                acc_prod(rh, rl, (float)v.y, 0.f, (float)x.y);
-                acc_prod(ih, il, (float)v.x, 0.f, (float)x.y);
-                acc_prod(ih, il, -(float)v.y, 0.f, (float)x.x);
+        }
+        for (; i + 32 < cl; i += 64) {
+            const C v = vk[i], u = vk[i + 32];
+            if (CACHE) {
+                cache[(size_t)k * chunk + i] = v;
+                cache[(size_t)k * chunk + i + 32] = u;
             }
-            ar = ((double)rh + (double)rl) + ((double)sh + (double)sl);
-            ai = ((double)ih + (double)il) + ((double)th + (double)tl);
-        } else {
-            const C* vk = V + (size_t)k * n + i0;
-            int i = lane;
-            for (; i + 96 < cl; i += 128) {
-                C v[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = vk[i + 32 * u];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    if (CACHE) cache[(size_t)k * chunk + i + 32 * u] = v[u];
-                    const C x = ws[i + 32 * u];
-                    if (u & 1) acc_dot64(br, bi, (double)v[u].x, (double)v[u].y, (double)x.x, (double)x.y);
-                    else acc_dot64(ar, ai, (double)v[u].x, (double)v[u].y, (double)x.x, (double)x.y);
-                }
-            }
-            for (; i + 32 < cl; i += 64) {
-                const C v = vk[i], u = vk[i + 32];
-                if (CACHE) {
-                    cache[(size_t)k * chunk + i] = v;
-                    cache[(size_t)k * chunk + i + 32] = u;
-                }
-                const C x = ws[i], y = ws[i + 32];
-                acc_dot64(ar, ai, (double)v.x, (double)v.y, (double)x.x, (double)x.y);
-                acc_dot64(br, bi, (double)u.x, (double)u.y, (double)y.x, (double)y.y);
-            }
-            if (i < cl) {
-                const C v = vk[i];
-                if (CACHE) cache[(size_t)k * chunk + i] = v;
-                const C x = ws[i];
-                acc_dot64(ar, ai, (double)v.x, (double)v.y, (double)x.x, (double)x.y);
-            }
+            const C x = ws[i], y = ws[i + 32];
+            acc_dot64(ar, ai, v.x, v.y, x.x, x.y);
+            acc_dot64(br, bi, u.x, u.y, y.x, y.y);
+        }
+        if (i < cl) {
+            const C v = vk[i];
+            if (CACHE) cache[(size_t)k * chunk + i] = v;
+            const C x = ws[i];
+            acc_dot64(ar, ai, v.x, v.y, x.x, x.y);
         }
         ar += br;
         ai += bi;
@@ -178,7 +130,6 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const cx<T>* __res
 
     // ---- phase B: h = sum of the partials (fixed order; tpv threads per value, a power of
     // two <= 32 so that each value's threads are consecutive lanes of one warp) --------------
-    __shared__ float2 hf[kMaxBasis + 1], hl[kMaxBasis + 1];
     {
         const int vals = 2 * nv;
         int tpv = 32;
@@ -200,76 +151,38 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const cx<T>* __res
         if (v < vals && q == 0) hs[v] = s;
     }
     __syncthreads();
-    if (kF32 && tid < nv) {
-        // FP32 hi / lo parts of h, formed once for the complex64 update
-        const float hr = (float)hs[2 * tid], hi = (float)hs[2 * tid + 1];
-        hf[tid] = make_float2(hr, hi);
-        hl[tid] = make_float2((float)(hs[2 * tid] - (double)hr), (float)(hs[2 * tid + 1] - (double)hi));
-    }
-    __syncthreads();
 
     double nrm = 0.0;
     if (update) {
         // w -= V h on this chunk; ||w||^2 partial
         for (int i = tid; i < cl; i += kFuseThreads) {
             C r = ws[i];
-            if (kF32) {
-                float sr = 0.f, si = 0.f, cr = 0.f, ci = 0.f;
-                int k = 0;
-                if (v0) {
-                    const double2 a = CACHE ? c0[i] : v0[i0 + i];
-                    const double hr = hs[0], hi = hs[1];
-                    // FP64 first vector: its product in FP64, folded into the remainder sum
-                    const double pr = a.x * hr - a.y * hi, pi = a.x * hi + a.y * hr;
-                    sr = (float)pr;
-                    si = (float)pi;
-                    cr = (float)(pr - (double)sr);
-                    ci = (float)(pi - (double)si);
-                    k = 1;
-                }
-                for (; k < nv; ++k) {
-                    const C vk = CACHE ? cache[(size_t)k * chunk + i] : V[(size_t)k * n + i0 + i];
-                    const float hr = hf[k].x, hi = hf[k].y, lr = hl[k].x, li = hl[k].y;
-                    sr = fmaf((float)vk.x, hr, sr);
-                    sr = fmaf(-(float)vk.y, hi, sr);
-                    si = fmaf((float)vk.x, hi, si);
-                    si = fmaf((float)vk.y, hr, si);
-                    cr = fmaf((float)vk.x, lr, cr);
-                    cr = fmaf(-(float)vk.y, li, cr);
-                    ci = fmaf((float)vk.x, li, ci);
-                    ci = fmaf((float)vk.y, lr, ci);
-                }
-                r.x = (T)((float)r.x - (sr + cr));
-                r.y = (T)((float)r.y - (si + ci));
-            } else {
-                double sr0 = 0.0, si0 = 0.0, sr1 = 0.0, si1 = 0.0;
-                int k = 0;
-                for (; k + 1 < nv; k += 2) {
-                    const C a = CACHE ? cache[(size_t)k * chunk + i] : V[(size_t)k * n + i0 + i];
-                    const C c = CACHE ? cache[(size_t)(k + 1) * chunk + i] : V[(size_t)(k + 1) * n + i0 + i];
-                    const double ar_ = (double)a.x, ai_ = (double)a.y, cr_ = (double)c.x, ci_ = (double)c.y;
-                    sr0 = fma(ar_, hs[2 * k], sr0);
-                    sr0 = fma(-ai_, hs[2 * k + 1], sr0);
-                    si0 = fma(ar_, hs[2 * k + 1], si0);
-                    si0 = fma(ai_, hs[2 * k], si0);
-                    sr1 = fma(cr_, hs[2 * k + 2], sr1);
-                    sr1 = fma(-ci_, hs[2 * k + 3], sr1);
-                    si1 = fma(cr_, hs[2 * k + 3], si1);
-                    si1 = fma(ci_, hs[2 * k + 2], si1);
-                }
-                if (k < nv) {
-                    const C a = CACHE ? cache[(size_t)k * chunk + i] : V[(size_t)k * n + i0 + i];
-                    sr0 = fma((double)a.x, hs[2 * k], sr0);
-                    sr0 = fma(-(double)a.y, hs[2 * k + 1], sr0);
-                    si0 = fma((double)a.x, hs[2 * k + 1], si0);
-                    si0 = fma((double)a.y, hs[2 * k], si0);
-                }
-                r.x -= (sr0 + sr1);
-                r.y -= (si0 + si1);
+            double sr0 = 0.0, si0 = 0.0, sr1 = 0.0, si1 = 0.0;
+            int k = 0;
+            for (; k + 1 < nv; k += 2) {
+                const C a = CACHE ? cache[(size_t)k * chunk + i] : V[(size_t)k * n + i0 + i];
+                const C c = CACHE ? cache[(size_t)(k + 1) * chunk + i] : V[(size_t)(k + 1) * n + i0 + i];
+                sr0 = fma(a.x, hs[2 * k], sr0);
+                sr0 = fma(-a.y, hs[2 * k + 1], sr0);
+                si0 = fma(a.x, hs[2 * k + 1], si0);
+                si0 = fma(a.y, hs[2 * k], si0);
+                sr1 = fma(c.x, hs[2 * k + 2], sr1);
+                sr1 = fma(-c.y, hs[2 * k + 3], sr1);
+                si1 = fma(c.x, hs[2 * k + 3], si1);
+                si1 = fma(c.y, hs[2 * k + 2], si1);
             }
+            if (k < nv) {
+                const C a = CACHE ? cache[(size_t)k * chunk + i] : V[(size_t)k * n + i0 + i];
+                sr0 = fma(a.x, hs[2 * k], sr0);
+                sr0 = fma(-a.y, hs[2 * k + 1], sr0);
+                si0 = fma(a.x, hs[2 * k + 1], si0);
+                si0 = fma(a.y, hs[2 * k], si0);
+            }
+            r.x -= (sr0 + sr1);
+            r.y -= (si0 + si1);
             w[i0 + i] = r;
-            nrm = fma((double)r.x, (double)r.x, nrm);
-            nrm = fma((double)r.y, (double)r.y, nrm);
+            nrm = fma(r.x, r.x, nrm);
+            nrm = fma(r.y, r.y, nrm);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
@@ -316,7 +229,259 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const cx<T>* __res
                 H[2 * ((size_t)(J + 1) * m + J)] = beta;
                 H[2 * ((size_t)(J + 1) * m + J) + 1] = 0.0;
                 ctrl->beta = beta;
-                ctrl->inv_beta = 1.0 / beta;
+                set_inv_beta(ctrl, beta);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Complex64 basis (FP32-mixed path).  The same three phases, with every inner product,
+// partial sum and norm formed by error-free FP32 transformations (hi + lo pairs): on this
+// GPU the FP64 pipe retires two thread operations per clock per SM, so FP64 adds in
+// reductions (every lane of every warp) cost as much as the products themselves.  The
+// first vector comes split into FP32 pairs (v0s, float4 re_hi, im_hi, re_lo, im_lo);
+// partials are float4 (re_hi, re_lo, im_hi, im_lo) per (vector, CTA).  Only single
+// threads touch FP64 (the Hessenberg entries, beta).
+constexpr int kCgsWarps = kFuseThreads / 32;
+constexpr int kCgsItems = 64;
+
+// compensated butterfly over the warp: every lane ends with the same (hi, lo)
+__device__ __forceinline__ void warp_pair_sum(float& h, float& l) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+        acc_pair(h, l, oh, ol);
+    }
+}
+
+template <bool CACHE>
+__global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __restrict__ V,
+                                                                const float4* __restrict__ v0s, long n, int J,
+                                                                int m, float2* __restrict__ w,
+                                                                float4* __restrict__ part, unsigned* bar,
+                                                                Ctrl* ctrl, double* H, int update, int chunk) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float4 psum[kCgsItems];
+    __shared__ float2 hf[kMaxBasis + 1], hl[kMaxBasis + 1];
+    __shared__ double hs[2 * (kMaxBasis + 1)];
+    __shared__ float2 red[kCgsWarps];
+    if (ctrl->broken) return;                        // uniform: written only between launches
+    const int nv = J + 1, G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long i0 = (long)b * chunk;
+    const int cl = (int)max(0L, min((long)chunk, n - i0));
+    float2* ws = reinterpret_cast<float2*>(smem_raw);
+    float4* c0 = reinterpret_cast<float4*>(smem_raw + (((size_t)chunk * sizeof(float2) + 15) & ~(size_t)15));
+    float2* cache = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(c0) + (v0s ? (size_t)chunk * 16 : 0));
+    for (int i = tid; i < cl; i += kFuseThreads) ws[i] = w[i0 + i];
+    __syncthreads();
+
+    // ---- phase A: partials of conj(v_k) . w; with fewer vectors than warps each vector's
+    // chunk is cut into S slices (one warp each), summed in slice order afterwards
+    const int S = nv >= kCgsWarps ? 1 : max(1, min(kCgsWarps / nv, cl / 32));
+    const int sl = ((cl + S - 1) / S + 31) & ~31;
+    for (int it = warp; it < nv * S; it += kCgsWarps) {
+        const int k = it / S;
+        const int e0 = min(cl, (it % S) * sl), e1 = min(cl, e0 + sl);
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f, sh = 0.f, sl2 = 0.f, th = 0.f, tl = 0.f;
+        if (v0s && k == 0) {
+            for (int i = e0 + lane; i < e1; i += 32) {
+                const float4 a = v0s[i0 + i];
+                if (CACHE) c0[i] = a;
+                const float2 x = ws[i];
+                // conj(a) x with a = hi + lo: re = ar xr + ai xi, im = ar xi - ai xr
+                acc_prod(rh, rl, a.x, a.z, x.x);
+                acc_prod(sh, sl2, a.y, a.w, x.y);
+                acc_prod(ih, il, a.x, a.z, x.y);
+                acc_prod(th, tl, -a.y, -a.w, x.x);
+            }
+        } else {
+            const float2* vk = V + (size_t)k * n + i0;
+            int i = e0 + lane;
+            for (; i + 96 < e1; i += 128) {
+                float2 v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = vk[i + 32 * u];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (CACHE) cache[(size_t)k * chunk + i + 32 * u] = v[u];
+                    const float2 x = ws[i + 32 * u];
+                    if (u & 1) {
+                        acc_prod(sh, sl2, v[u].x, 0.f, x.x);
+                        acc_prod(sh, sl2, v[u].y, 0.f, x.y);
+                        acc_prod(th, tl, v[u].x, 0.f, x.y);
+                        acc_prod(th, tl, -v[u].y, 0.f, x.x);
+                    } else {
+                        acc_prod(rh, rl, v[u].x, 0.f, x.x);
+                        acc_prod(rh, rl, v[u].y, 0.f, x.y);
+                        acc_prod(ih, il, v[u].x, 0.f, x.y);
+                        acc_prod(ih, il, -v[u].y, 0.f, x.x);
+                    }
+                }
+            }
+            for (; i < e1; i += 32) {
+                const float2 v = vk[i];
+                if (CACHE) cache[(size_t)k * chunk + i] = v;
+                const float2 x = ws[i];
+                acc_prod(rh, rl, v.x, 0.f, x.x);
+                acc_prod(rh, rl, v.y, 0.f, x.y);
+                acc_prod(ih, il, v.x, 0.f, x.y);
+                acc_prod(ih, il, -v.y, 0.f, x.x);
+            }
+        }
+        acc_pair(rh, rl, sh, sl2);
+        acc_pair(ih, il, th, tl);
+        warp_pair_sum(rh, rl);
+        warp_pair_sum(ih, il);
+        if (lane == 0) {
+            const float4 r = make_float4(rh, rl, ih, il);
+            if (S == 1) part[(size_t)k * G + b] = r;
+            else psum[it] = r;
+        }
+    }
+    if (S > 1) {
+        __syncthreads();
+        if (tid < nv) {
+            float4 a = psum[tid * S];
+            for (int q = 1; q < S; ++q) {
+                const float4 c = psum[tid * S + q];
+                acc_pair(a.x, a.y, c.x, c.y);
+                acc_pair(a.z, a.w, c.z, c.w);
+            }
+            part[(size_t)tid * G + b] = a;
+        }
+    }
+    if (!grid_barrier(bar, G, ctrl)) return;
+
+    // ---- phase B: h_k = sum over the CTAs' partials, every CTA in the same fixed order:
+    // tpv consecutive lanes per vector, lane q taking partials q, q + tpv, ... (four loads in
+    // flight), then a compensated shuffle tree inside the group
+    {
+        int tpv = 32;
+        while (tpv > 1 && tpv * nv > kFuseThreads) tpv >>= 1;
+        const int k = tid / tpv, q = tid % tpv;
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+        if (k < nv) {
+            const float4* p = part + (size_t)k * G;
+            int g = q;
+            for (; g + 3 * tpv < G; g += 4 * tpv) {
+                float4 c[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) c[u] = __ldcg(p + g + u * tpv);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    acc_pair(rh, rl, c[u].x, c[u].y);
+                    acc_pair(ih, il, c[u].z, c[u].w);
+                }
+            }
+            for (; g < G; g += tpv) {
+                const float4 c = __ldcg(p + g);
+                acc_pair(rh, rl, c.x, c.y);
+                acc_pair(ih, il, c.z, c.w);
+            }
+        }
+        for (int o = 1; o < tpv; o <<= 1) {
+            const float a = __shfl_xor_sync(0xffffffffu, rh, o), c = __shfl_xor_sync(0xffffffffu, rl, o);
+            const float d = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
+            acc_pair(rh, rl, a, c);
+            acc_pair(ih, il, d, e);
+        }
+        if (k < nv && q == 0) {
+            float h1, l1, h2, l2;
+            two_sum(rh, rl, h1, l1);                 // normalised pairs
+            two_sum(ih, il, h2, l2);
+            hf[k] = make_float2(h1, h2);
+            hl[k] = make_float2(l1, l2);
+            hs[2 * k] = (double)h1 + (double)l1;
+            hs[2 * k + 1] = (double)h2 + (double)l2;
+        }
+    }
+    __syncthreads();
+
+    if (update) {
+        // w -= V h on this chunk (the first vector's product to first order in the low
+        // parts); ||w||^2 partial as an exact-square compensated sum
+        float nh = 0.f, nl = 0.f;
+        for (int i = tid; i < cl; i += kFuseThreads) {
+            float2 r = ws[i];
+            float sr = 0.f, si = 0.f, cr = 0.f, ci = 0.f;
+            int k = 0;
+            if (v0s) {
+                const float4 a = CACHE ? c0[i] : v0s[i0 + i];
+                const float2 H0 = hf[0], L0 = hl[0];
+                acc_prod(sr, cr, H0.x, L0.x, a.x);
+                acc_prod(sr, cr, -H0.y, -L0.y, a.y);
+                acc_prod(si, ci, H0.y, L0.y, a.x);
+                acc_prod(si, ci, H0.x, L0.x, a.y);
+                cr = __fmaf_rn(a.z, H0.x, __fmaf_rn(-a.w, H0.y, cr));
+                ci = __fmaf_rn(a.z, H0.y, __fmaf_rn(a.w, H0.x, ci));
+                k = 1;
+            }
+            for (; k < nv; ++k) {
+                const float2 vk = CACHE ? cache[(size_t)k * chunk + i] : V[(size_t)k * n + i0 + i];
+                const float2 Hk = hf[k], Lk = hl[k];
+                sr = fmaf(vk.x, Hk.x, sr);
+                sr = fmaf(-vk.y, Hk.y, sr);
+                si = fmaf(vk.x, Hk.y, si);
+                si = fmaf(vk.y, Hk.x, si);
+                cr = fmaf(vk.x, Lk.x, cr);
+                cr = fmaf(-vk.y, Lk.y, cr);
+                ci = fmaf(vk.x, Lk.y, ci);
+                ci = fmaf(vk.y, Lk.x, ci);
+            }
+            r.x = r.x - (sr + cr);
+            r.y = r.y - (si + ci);
+            w[i0 + i] = r;
+            acc_prod(nh, nl, r.x, 0.f, r.x);
+            acc_prod(nh, nl, r.y, 0.f, r.y);
+        }
+        warp_pair_sum(nh, nl);
+        if (lane == 0) red[warp] = make_float2(nh, nl);
+        __syncthreads();
+        if (tid == 0) {
+            float a = 0.f, c = 0.f;
+            for (int q = 0; q < kCgsWarps; ++q) acc_pair(a, c, red[q].x, red[q].y);
+            part[(size_t)nv * G + b] = make_float4(a, c, 0.f, 0.f);
+        }
+        if (!grid_barrier(bar, G, ctrl)) return;
+    }
+
+    // ---- phase C: Hessenberg column, beta and the breakdown test (CTA 0) --------------------
+    if (b != 0) return;
+    __shared__ double s_beta;
+    if (update && warp == 0) {
+        float a = 0.f, c = 0.f;
+        for (int g = lane; g < G; g += 32) {
+            const float4 t = __ldcg(part + (size_t)nv * G + g);
+            acc_pair(a, c, t.x, t.y);
+        }
+        warp_pair_sum(a, c);
+        if (lane == 0) s_beta = sqrt((double)a + (double)c);
+    }
+    __syncthreads();
+    for (int k = tid; k < nv; k += kFuseThreads) {
+        H[2 * ((size_t)k * m + J)] = hs[2 * k];
+        H[2 * ((size_t)k * m + J) + 1] = hs[2 * k + 1];
+        ctrl->h[2 * k] = hs[2 * k];
+        ctrl->h[2 * k + 1] = hs[2 * k + 1];
+    }
+    if (tid == 0) {
+        ctrl->nbasis = nv;
+        ctrl->operator_count++;
+        if (J == 0) ctrl->inner_product_count++;
+        if (J + 1 < m) {
+            const double beta = s_beta;
+            ctrl->resid_norm = beta;
+            const double tol = sqrt(DBL_EPSILON);   // pamp.h:79
+            if (!isfinite(beta)) ctrl->nonfinite = 1;
+            if (fabs(beta) < tol) {
+                ctrl->broken = 1;
+                ctrl->breakdown_count++;
+            } else {
+                H[2 * ((size_t)(J + 1) * m + J)] = beta;
+                H[2 * ((size_t)(J + 1) * m + J) + 1] = 0.0;
+                ctrl->beta = beta;
+                set_inv_beta(ctrl, beta);
             }
         }
     }
@@ -331,12 +496,8 @@ size_t arnoldi_cgs_smem(int prec, long n, int nv, int grid, int with_v0, int cac
     return b;
 }
 
-template <typename T, bool CACHE>
-static cudaError_t arnoldi_cgs_launch(const void* V, const double2* v0, long n, int J, int m, void* w, double* part,
-                                      unsigned* bar, Ctrl* ctrl, double* H, int update, int grid, cudaStream_t s) {
-    const int chunk = (int)(((n + grid - 1) / grid + 7) / 8 * 8);
-    const size_t smem = arnoldi_cgs_smem(sizeof(T) == 8 ? 0 : 1, n, J + 1, grid, v0 != nullptr, CACHE);
-    auto kern = k_arnoldi_cgs<T, CACHE>;
+template <typename Kern, typename... Args>
+static cudaError_t cgs_coop_launch(Kern kern, int grid, size_t smem, cudaStream_t s, Args... args) {
     cudaError_t e = allow_max_smem(kern);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
@@ -349,18 +510,23 @@ static cudaError_t arnoldi_cgs_launch(const void* V, const double2* v0, long n, 
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, (const cx<T>*)V, v0, n, J, m, (cx<T>*)w, part, bar, ctrl, H, update, chunk);
+    return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
-cudaError_t launch_arnoldi_cgs(int prec, const void* V, const double2* v0, long n, int J, int m, void* w,
+cudaError_t launch_arnoldi_cgs(int prec, const void* V, const void* v0, long n, int J, int m, void* w,
                                double* part, unsigned* bar, Ctrl* ctrl, double* H, int update, int grid, int cache,
                                cudaStream_t s) {
     count_launch();
-    if (prec == 0)
-        return cache ? arnoldi_cgs_launch<double, true>(V, nullptr, n, J, m, w, part, bar, ctrl, H, update, grid, s)
-                     : arnoldi_cgs_launch<double, false>(V, nullptr, n, J, m, w, part, bar, ctrl, H, update, grid, s);
-    return cache ? arnoldi_cgs_launch<float, true>(V, v0, n, J, m, w, part, bar, ctrl, H, update, grid, s)
-                 : arnoldi_cgs_launch<float, false>(V, v0, n, J, m, w, part, bar, ctrl, H, update, grid, s);
+    const int chunk = (int)(((n + grid - 1) / grid + 7) / 8 * 8);
+    const size_t smem = arnoldi_cgs_smem(prec, n, J + 1, grid, v0 != nullptr, cache);
+    if (prec == 0) {
+        auto kern = cache ? k_arnoldi_cgs<true> : k_arnoldi_cgs<false>;
+        return cgs_coop_launch(kern, grid, smem, s, (const double2*)V, n, J, m, (double2*)w, part, bar, ctrl, H, update,
+                               chunk);
+    }
+    auto kern = cache ? k_arnoldi_cgs32<true> : k_arnoldi_cgs32<false>;
+    return cgs_coop_launch(kern, grid, smem, s, (const float2*)V, (const float4*)v0, n, J, m, (float2*)w,
+                           (float4*)part, bar, ctrl, H, update, chunk);
 }
 
 // Largest grid of co-resident CTAs for this configuration (0 when the cooperative form
@@ -377,11 +543,11 @@ int arnoldi_cgs_grid(int prec, long n, int m, int with_v0, int cache) {
     int per_sm = 0;
     cudaError_t e;
     if (prec == 0) {
-        auto kern = cache ? k_arnoldi_cgs<double, true> : k_arnoldi_cgs<double, false>;
+        auto kern = cache ? k_arnoldi_cgs<true> : k_arnoldi_cgs<false>;
         allow_max_smem(kern);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFuseThreads, smem);
     } else {
-        auto kern = cache ? k_arnoldi_cgs<float, true> : k_arnoldi_cgs<float, false>;
+        auto kern = cache ? k_arnoldi_cgs32<true> : k_arnoldi_cgs32<false>;
         allow_max_smem(kern);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFuseThreads, smem);
     }

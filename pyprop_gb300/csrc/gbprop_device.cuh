@@ -57,6 +57,29 @@ __device__ __forceinline__ void acc_scaled(float& hi, float& lo, float ch, float
     lo = __fadd_rn(lo, __fadd_rn(t, __fadd_rn(pe, __fmaf_rn(ch, sl, __fmul_rn(cl, sh)))));
 }
 
+// (hi, lo) += (bh + bl)
+__device__ __forceinline__ void acc_pair(float& hi, float& lo, float bh, float bl) {
+    float t;
+    two_sum(hi, bh, hi, t);
+    lo = __fadd_rn(lo, __fadd_rn(bl, t));
+}
+
+// x * (h + l) rounded once to FP32 (exact product x*h, the low part to first order)
+__device__ __forceinline__ float mul_pair(float x, float h, float l) {
+    const float p = __fmul_rn(x, h);
+    const float e = __fmaf_rn(x, h, -p);
+    return __fadd_rn(p, __fmaf_rn(x, l, e));
+}
+
+// 1 / beta for the next basis vector: FP64, and as an FP32 pair for the complex64 solve
+__device__ __forceinline__ void set_inv_beta(Ctrl* c, double beta) {
+    const double ib = 1.0 / beta;
+    c->inv_beta = ib;
+    const float h = (float)ib;
+    c->inv_beta_f[0] = h;
+    c->inv_beta_f[1] = (float)(ib - (double)h);
+}
+
 // Programmatic dependent launch: a kernel launched with launch_pdl is scheduled as its
 // predecessor's CTAs retire (no explicit early trigger: CTAs of the next kernel waiting on
 // SMs slowed the solve measurably), hiding the launch gap between stream-launched kernels;

@@ -127,6 +127,7 @@ struct Ctrl {
     double beta0;           // ||U psi|| at the start of the step
     double beta;            // current residual norm
     double inv_beta;        // 1 / beta (the reference scales by the reciprocal)
+    float inv_beta_f[2];    // inv_beta as an FP32 pair (hi, lo) for the complex64 solve
     double orig_norm;       // ||w|| before Gram-Schmidt (re-orthogonalisation rule; updated per pass)
     double pre_norm;        // ||w|| of the operator output, before any Gram-Schmidt pass
     double resid_norm;      // ||w|| after Gram-Schmidt
@@ -169,9 +170,11 @@ cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, cons
 // refine64 is set (FP64-accurate result).  refine64 = 0 is the complex64 solve of the mixed
 // path's Krylov basis: one refinement whose residual is formed with error-free FP32 products
 // and sums, complex64 output.  Grid: (tab.nchunks, nrows); arguments as launch_solve.
+// v0s (complex64 solve of the FP64 first vector only, may be null) receives the scaled input
+// split into FP32 pairs, float4 (re_hi, im_hi, re_lo, im_lo) per element.
 cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
                              int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
-                             int check_broken, cudaStream_t s);
+                             int check_broken, cudaStream_t s, float4* v0s = nullptr);
 cudaError_t launch_band_apply(int arith, const void* op, const void* x, void* y, const SchedEntry* sched,
                               const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s);
 cudaError_t launch_tbmv(int arith, int kd, const void* ud_phys, int nl, int nr, const void* in, int in_prec,
@@ -197,7 +200,9 @@ cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int dou
 // arnoldi_cgs_part_doubles(grid) doubles; bar: two words, zero before the first launch.
 // update = 0 forms only the Hessenberg column (last vector).  cache: keep V's chunk in
 // shared memory between the two passes.
-cudaError_t launch_arnoldi_cgs(int prec, const void* V, const double2* v0, long n, int J, int m, void* w,
+// The complex64 form takes the first vector as FP32 pairs (v0s, see launch_solve_inv) and
+// forms every sum with error-free FP32 transformations.
+cudaError_t launch_arnoldi_cgs(int prec, const void* V, const void* v0, long n, int J, int m, void* w,
                                double* part, unsigned* bar, Ctrl* ctrl, double* H, int update, int grid, int cache,
                                cudaStream_t s);
 // Grid size for the cooperative Gram-Schmidt (0 if it cannot run co-resident).

@@ -154,6 +154,22 @@ __host__ __device__ constexpr int band_threads(int v) {
 }
 __host__ __device__ constexpr int band_per(int v) { return v == 0 ? 2 : v == 1 ? 2 : v == 2 ? 4 : 1; }
 
+// Term factor coef_t * (s if time-dependent) of term t, formed by one thread per CTA and
+// shared: FP64 (cr, ci) for the FP64 band, the FP32 pairs (Cr, Crl, Ci, Cil) for the
+// complex64 band.  Per thread this was ~10 FP64 instructions per term, a large share of
+// the complex64 kernel on a GPU whose FP64 pipe retires two thread operations per clock.
+template <typename T>
+__device__ __forceinline__ void band_term_coef(const BandOp<T>& op, int t, double scal, double2* cd, float4* cf) {
+    double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
+    if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
+    if constexpr (sizeof(T) == sizeof(double)) {
+        *cd = make_double2(cr, ci);
+    } else {
+        const float a = (float)cr, b = (float)ci;
+        *cf = make_float4(a, (float)(cr - (double)a), b, (float)(ci - (double)b));
+    }
+}
+
 // One block: destination row l = blockIdx.y, radial tile blockIdx.x.  For every term
 // of row l the source row's tile (with a kb halo) is staged in shared memory; each
 // thread accumulates PER elements with the band sum split into even/odd diagonals
@@ -167,11 +183,12 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
     constexpr int W = 2 * KB + 1;
     constexpr int TILE = THREADS * PER;
     __shared__ C sx[TILE + 2 * KB];
+    __shared__ double2 s_cd;
+    __shared__ float4 s_cf;
     pdl_wait();
     if (check_broken && ctrl->broken) return;
     const int l = blockIdx.y, i0 = blockIdx.x * TILE, tid = threadIdx.x;
     const int nr = op.nr;
-    const double scal = sched ? sched[ctrl->step].scaling : scal_val;
     const bool kSplit = sizeof(T) < sizeof(double) && op.slots_lo != nullptr;
     T yr[PER], yi[PER], zr[PER], zi[PER];
 #pragma unroll
@@ -184,11 +201,12 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
             const int g = i0 - KB + j;
             sx[j] = (g >= 0 && g < nr) ? x[sbase + g] : mk<T>(0, 0);
         }
+        if (tid == 0) band_term_coef(op, t, sched ? sched[ctrl->step].scaling : scal_val, &s_cd, &s_cf);
         __syncthreads();
         const T* A = op.slots + (size_t)op.t_slot[t] * W * nr;
-        double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
-        if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
-        const T Cr = (T)cr, Ci = (T)ci;
+        T Cr, Ci;
+        if constexpr (sizeof(T) == sizeof(double)) { Cr = s_cd.x; Ci = s_cd.y; }
+        else { Cr = s_cf.x; Ci = s_cf.z; }
         if constexpr (sizeof(T) < sizeof(double)) {
             if (kSplit) {
                 // complex64 path: error-free products and compensated sums of the band
@@ -196,7 +214,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
                 // operator applied to the complex64 source, rounded once.  The kinetic band's
                 // large alternating entries make plain FP32 sums lose ~eps32 * sum|a s|.
                 const float* Alo = op.slots_lo + (size_t)op.t_slot[t] * W * nr;
-                const float Crl = (float)(cr - (double)Cr), Cil = (float)(ci - (double)Ci);
+                const float Crl = s_cf.y, Cil = s_cf.w;
 #pragma unroll
                 for (int e = 0; e < PER; ++e) {
                     const int li = tid + e * THREADS;
@@ -279,71 +297,82 @@ __global__ void __launch_bounds__(THREADS) k_band_apply_l1(BandOp<T> op, const c
                                                            int check_broken) {
     using C = cx<T>;
     constexpr int W = 2 * KB + 1;
+    constexpr int kTerms = 32;                      // term factors staged per round
+    __shared__ double2 s_cd[kTerms];
+    __shared__ float4 s_cf[kTerms];
     pdl_wait();
     if (check_broken && ctrl->broken) return;
     const int l = blockIdx.y, nr = op.nr;
     const int i = blockIdx.x * THREADS + threadIdx.x;
-    if (i >= nr) return;
-    const double scal = sched ? sched[ctrl->step].scaling : scal_val;
+    const bool active = i < nr;
     const bool split = sizeof(T) < sizeof(double) && op.slots_lo != nullptr;
     T yr = 0, yi = 0, zr = 0, zi = 0;
     const int t0 = op.row_ptr[l], t1 = op.row_ptr[l + 1];
-    for (int t = t0; t < t1; ++t) {
-        const C* xs = x + (size_t)op.t_src[t] * nr;
-        const T* A = op.slots + (size_t)op.t_slot[t] * W * nr;
-        double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
-        if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
-        const T Cr = (T)cr, Ci = (T)ci;
-        C v[W];
+    for (int tg = t0; tg < t1; tg += kTerms) {
+        const int tn = min(kTerms, t1 - tg);
+        if (tg > t0) __syncthreads();
+        if ((int)threadIdx.x < tn)
+            band_term_coef(op, tg + threadIdx.x, sched ? sched[ctrl->step].scaling : scal_val, &s_cd[threadIdx.x],
+                           &s_cf[threadIdx.x]);
+        __syncthreads();
+        if (!active) continue;
+        for (int t = tg; t < tg + tn; ++t) {
+            const C* xs = x + (size_t)op.t_src[t] * nr;
+            const T* A = op.slots + (size_t)op.t_slot[t] * W * nr;
+            T Cr, Ci;
+            if constexpr (sizeof(T) == sizeof(double)) { Cr = s_cd[t - tg].x; Ci = s_cd[t - tg].y; }
+            else { Cr = s_cf[t - tg].x; Ci = s_cf[t - tg].z; }
+            C v[W];
 #pragma unroll
-        for (int d = 0; d < W; ++d) {
-            const int g = i + d - KB;
-            v[d] = (g >= 0 && g < nr) ? __ldg(xs + g) : mk<T>(0, 0);
-        }
-        if constexpr (sizeof(T) < sizeof(double)) {
-            if (split) {
-                const float* Alo = op.slots_lo + (size_t)op.t_slot[t] * W * nr;
-                const float Crl = (float)(cr - (double)Cr), Cil = (float)(ci - (double)Ci);
-                float srh = 0.f, srl = 0.f, sih = 0.f, sil = 0.f, orh = 0.f, orl = 0.f, oih = 0.f, oil = 0.f;
-#pragma unroll
-                for (int d = 0; d < W; ++d) {
-                    const float a = __ldg(A + (size_t)d * nr + i), al = __ldg(Alo + (size_t)d * nr + i);
-                    if (d & 1) {
-                        acc_prod(orh, orl, a, al, v[d].x);
-                        acc_prod(oih, oil, a, al, v[d].y);
-                    } else {
-                        acc_prod(srh, srl, a, al, v[d].x);
-                        acc_prod(sih, sil, a, al, v[d].y);
-                    }
-                }
-                float tt;
-                two_sum(srh, orh, srh, tt);
-                srl = __fadd_rn(__fadd_rn(srl, orl), tt);
-                two_sum(sih, oih, sih, tt);
-                sil = __fadd_rn(__fadd_rn(sil, oil), tt);
-                if (Cr != 0.f || Crl != 0.f) {
-                    acc_scaled(yr, zr, Cr, Crl, srh, srl);
-                    acc_scaled(yi, zi, Cr, Crl, sih, sil);
-                }
-                if (Ci != 0.f || Cil != 0.f) {
-                    acc_scaled(yr, zr, -Ci, -Cil, sih, sil);
-                    acc_scaled(yi, zi, Ci, Cil, srh, srl);
-                }
-                continue;
+            for (int d = 0; d < W; ++d) {
+                const int g = i + d - KB;
+                v[d] = (g >= 0 && g < nr) ? __ldg(xs + g) : mk<T>(0, 0);
             }
-        }
-        T ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
+            if constexpr (sizeof(T) < sizeof(double)) {
+                if (split) {
+                    const float* Alo = op.slots_lo + (size_t)op.t_slot[t] * W * nr;
+                    const float Crl = s_cf[t - tg].y, Cil = s_cf[t - tg].w;
+                    float srh = 0.f, srl = 0.f, sih = 0.f, sil = 0.f, orh = 0.f, orl = 0.f, oih = 0.f, oil = 0.f;
 #pragma unroll
-        for (int d = 0; d < W; ++d) {
-            const T a = __ldg(A + (size_t)d * nr + i);
-            if (d & 1) { ar1 = fma(a, v[d].x, ar1); ai1 = fma(a, v[d].y, ai1); }
-            else { ar0 = fma(a, v[d].x, ar0); ai0 = fma(a, v[d].y, ai0); }
+                    for (int d = 0; d < W; ++d) {
+                        const float a = __ldg(A + (size_t)d * nr + i), al = __ldg(Alo + (size_t)d * nr + i);
+                        if (d & 1) {
+                            acc_prod(orh, orl, a, al, v[d].x);
+                            acc_prod(oih, oil, a, al, v[d].y);
+                        } else {
+                            acc_prod(srh, srl, a, al, v[d].x);
+                            acc_prod(sih, sil, a, al, v[d].y);
+                        }
+                    }
+                    float tt;
+                    two_sum(srh, orh, srh, tt);
+                    srl = __fadd_rn(__fadd_rn(srl, orl), tt);
+                    two_sum(sih, oih, sih, tt);
+                    sil = __fadd_rn(__fadd_rn(sil, oil), tt);
+                    if (Cr != 0.f || Crl != 0.f) {
+                        acc_scaled(yr, zr, Cr, Crl, srh, srl);
+                        acc_scaled(yi, zi, Cr, Crl, sih, sil);
+                    }
+                    if (Ci != 0.f || Cil != 0.f) {
+                        acc_scaled(yr, zr, -Ci, -Cil, sih, sil);
+                        acc_scaled(yi, zi, Ci, Cil, srh, srl);
+                    }
+                    continue;
+                }
+            }
+            T ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
+#pragma unroll
+            for (int d = 0; d < W; ++d) {
+                const T a = __ldg(A + (size_t)d * nr + i);
+                if (d & 1) { ar1 = fma(a, v[d].x, ar1); ai1 = fma(a, v[d].y, ai1); }
+                else { ar0 = fma(a, v[d].x, ar0); ai0 = fma(a, v[d].y, ai0); }
+            }
+            const T ar = ar0 + ar1, ai = ai0 + ai1;
+            yr += Cr * ar - Ci * ai;
+            yi += Cr * ai + Ci * ar;
         }
-        const T ar = ar0 + ar1, ai = ai0 + ai1;
-        yr += Cr * ar - Ci * ai;
-        yi += Cr * ai + Ci * ar;
     }
-    y[(size_t)l * nr + i] = mk<T>(yr + zr, yi + zi);
+    if (active) y[(size_t)l * nr + i] = mk<T>(yr + zr, yi + zi);
 }
 
 template <typename T, int KB, int V>
@@ -480,7 +509,7 @@ __global__ void __launch_bounds__(kRedThreads) k_norm(const CI* __restrict__ x, 
             const double b = sqrt(tot[0]);
             ctrl->beta0 = b;
             ctrl->beta = b;
-            ctrl->inv_beta = 1.0 / b;
+            set_inv_beta(ctrl, b);
             if (!isfinite(b) || b == 0.0) ctrl->nonfinite = 1;
             *counter = 0;
         }
@@ -843,7 +872,7 @@ __global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int doub
                 H[2 * ((size_t)(J + 1) * m + J)] = beta;
                 H[2 * ((size_t)(J + 1) * m + J) + 1] = 0.0;
                 ctrl->beta = beta;
-                ctrl->inv_beta = 1.0 / beta;
+                set_inv_beta(ctrl, beta);
             }
         }
     }

@@ -625,7 +625,7 @@ template <int KD, bool STAGE, typename TI, typename TV>
 __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const TI* __restrict__ in,
                                                              float2* __restrict__ out, TV* __restrict__ vstore,
                                                              Ctrl* __restrict__ ctrl, int dir, int scale_mode,
-                                                             int check_broken) {
+                                                             int check_broken, float4* __restrict__ v0s) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long s_bar;
     const int n = tab.n, w = tab.w;
@@ -675,26 +675,46 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
     const float* uhb = STAGE ? Uh : Uhg;
     const float* ulb = STAGE ? Ul : Ulg;
     const size_t ustride = STAGE ? (size_t)R0p : (size_t)tab.npad;
-    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
     const size_t base = (size_t)l * n;
     constexpr bool kWide = sizeof(TI) == sizeof(double2);
-    for (int q = tid; q < R0 + w; q += kInvThreads) {
-        float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
-        if (q < RB) {
-            const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-            const TI t = in[base + p];
-            double2 b = make_double2((double)t.x, (double)t.y);
-            if (scale_mode) { b.x *= sc; b.y *= sc; }
-            hi = make_float2((float)b.x, (float)b.y);
-            if (kWide) lo = make_float2((float)(b.x - (double)hi.x), (float)(b.y - (double)hi.y));
-            if (vstore && q < cl) {
-                if (sizeof(TV) == sizeof(double2)) vstore[base + p] = conv<TV>(b);
-                else vstore[base + p] = conv<TV>(hi);
+    if constexpr (kWide) {
+        // the FP64 first vector (once per step): scaled in FP64, kept as hi + lo
+        const double sc = scale_mode ? ctrl->inv_beta : 1.0;
+        for (int q = tid; q < R0 + w; q += kInvThreads) {
+            float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
+            if (q < RB) {
+                const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+                const TI t = in[base + p];
+                double2 b = make_double2((double)t.x, (double)t.y);
+                if (scale_mode) { b.x *= sc; b.y *= sc; }
+                hi = make_float2((float)b.x, (float)b.y);
+                lo = make_float2((float)(b.x - (double)hi.x), (float)(b.y - (double)hi.y));
+                if (q < cl) {
+                    if (vstore) vstore[base + p] = conv<TV>(b);
+                    if (v0s) v0s[base + p] = make_float4(hi.x, hi.y, lo.x, lo.y);
+                }
+                bh[q] = hi;
+                bl[q] = lo;
             }
-            bh[q] = hi;
-            bl[q] = lo;
+            r32[q] = hi;
         }
-        r32[q] = hi;
+    } else {
+        // a complex64 vector: scaled by 1/beta as an FP32 pair, rounded once (no FP64
+        // instruction per element)
+        const float sh = scale_mode ? ctrl->inv_beta_f[0] : 1.f, sl = scale_mode ? ctrl->inv_beta_f[1] : 0.f;
+        for (int q = tid; q < R0 + w; q += kInvThreads) {
+            float2 hi = make_float2(0.f, 0.f);
+            if (q < RB) {
+                const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+                const TI t = in[base + p];
+                hi = make_float2((float)t.x, (float)t.y);
+                if (scale_mode) hi = make_float2(mul_pair(hi.x, sh, sl), mul_pair(hi.y, sh, sl));
+                if (vstore && q < cl) vstore[base + p] = conv<TV>(hi);
+                bh[q] = hi;
+                bl[q] = make_float2(0.f, 0.f);
+            }
+            r32[q] = hi;
+        }
     }
     bool ok = true;
     if (STAGE) ok = mbar_wait0(&s_bar);
@@ -740,7 +760,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
 template <int KD, bool STAGE>
 static cudaError_t solve_mixed_launch(const InvTab& tab, int nrows, const void* in, int in_prec, void* out,
                                       int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
-                                      int check_broken, cudaStream_t s) {
+                                      int check_broken, cudaStream_t s, float4* v0s) {
     if (out_prec != 1) return cudaErrorInvalidValue;
     size_t smem = 0;
     for (int c = 0; c < tab.nchunks; ++c)
@@ -754,11 +774,12 @@ static cudaError_t solve_mixed_launch(const InvTab& tab, int nrows, const void* 
             if (ea != cudaSuccess) return ea;                                                                    \
         }                                                                                                        \
         cudaError_t el = launch_pdl(kern, grid, block, smem, s, tab, (const TI_*)in, (float2*)out, (TV_*)vstore,  \
-                                    ctrl, dir, scale_mode, check_broken);                                        \
+                                    ctrl, dir, scale_mode, check_broken, v0s);                                   \
         return el != cudaSuccess ? el : cudaGetLastError();                                                      \
     }
     // in: the FP64 first vector (with its FP64 copy stored) or a complex64 vector
     if (in_prec == 0 && v_prec == 0) GB_MIX_CASE(double2, double2)
+    if (v0s) return cudaErrorInvalidValue;
     if (in_prec == 1) GB_MIX_CASE(float2, float2)
 #undef GB_MIX_CASE
     return cudaErrorInvalidValue;
@@ -799,7 +820,7 @@ static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in
 template <int KD>
 static cudaError_t solve_inv_kd(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
                                 int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
-                                int check_broken, cudaStream_t s) {
+                                int check_broken, cudaStream_t s, float4* v0s) {
     if (refine64) {
         if (tab.stage)
             return solve_inv_launch<KD, true, true>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
@@ -809,20 +830,20 @@ static cudaError_t solve_inv_kd(const InvTab& tab, int nrows, int refine64, cons
     }
     if (tab.stage)
         return solve_mixed_launch<KD, true>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
-                                            scale_mode, check_broken, s);
+                                            scale_mode, check_broken, s, v0s);
     return solve_mixed_launch<KD, false>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
-                                         scale_mode, check_broken, s);
+                                         scale_mode, check_broken, s, v0s);
 }
 
 cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
                              int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
-                             int check_broken, cudaStream_t s) {
+                             int check_broken, cudaStream_t s, float4* v0s) {
     count_launch();
     switch (tab.kd) {
 #define GB_KD(K)                                                                                                 \
     case K:                                                                                                      \
         return solve_inv_kd<K>(tab, nrows, refine64, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,      \
-                               scale_mode, check_broken, s);
+                               scale_mode, check_broken, s, v0s);
         GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
 #undef GB_KD
         default: return cudaErrorInvalidValue;
