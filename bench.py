@@ -532,6 +532,7 @@ def measure_single(args, precision, device, world, with_e2e=True):
     torch.cuda.synchronize()
     _barrier(world)
     launches = _native.launch_count() - launches0
+    sorder = int(h.stats().last_scaling_order)
     ms = sum(s_.elapsed_time(e) for s_, e in zip(starts, ends))
     clk = clocks.stop()
     ms = _max_over_ranks(ms, world)
@@ -604,7 +605,7 @@ def measure_single(args, precision, device, world, with_e2e=True):
         "config": {"workload": "hydrogen_velocity_%s" % args.workload, "nl": nl, "nr": nr, "order": 7, "m": m,
                    "dt": dt.real, "precision": precision, "l2": "flushed between steps (%d MB write)" % args.flush_mb,
                    "parallelism": "replicas" if world > 1 else "single", "inverse_band": w,
-                   "band_variant": prob.Propagator.BandVariant},
+                   "band_variant": prob.Propagator.BandVariant, "expm_scaling_order": sorder},
         "e2e": e2e,
         "roofline": roofline,
         "step_bytes": {"algorithmic_per_step": B_step, "achieved_GBps": B_step * value / world / 1e9,

@@ -20,32 +20,34 @@ namespace gbprop {
 constexpr int kFuseThreads = 512;
 constexpr long kBarrierSpinLimit = 1L << 24;   // polls (each an L2 round trip) before a barrier gives up
 
-// Sense-reversing grid barrier for a co-resident grid: bar[0] = arrivals, bar[1] = generation.
-// Bounded: after kBarrierSpinLimit polls it records ctrl->wait_timeout and returns false.
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, Ctrl* ctrl) {
+// Grid barrier for a co-resident grid on a counter that only grows within an Arnoldi step
+// (zeroed before the step's first launch): barrier number t of the step completes when the
+// counter reaches (t + 1) * nblocks.  One acquire-release atomic per CTA and acquire polls
+// (1.2 us per barrier over 152 CTAs, against 2.3 us with full fences around a volatile
+// sense flag).  Bounded: after kBarrierSpinLimit polls it records ctrl->wait_timeout and
+// returns false.
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, unsigned t, Ctrl* ctrl) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        volatile unsigned* gen = bar + 1;
-        const unsigned g = *gen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            long it = 0;
-            while (*gen == g) {
-                if (++it > kBarrierSpinLimit) {
-                    ctrl->wait_timeout = 1;
-                    ok = 0;
-                    break;
-                }
+        unsigned old;
+        asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(bar) : "memory");
+        const unsigned target = (t + 1) * nblocks;
+        long it = 0;
+        while ((int)(ld_acquire_gpu(bar) - target) < 0) {
+            if (++it > kBarrierSpinLimit) {
+                ctrl->wait_timeout = 1;
+                ok = 0;
+                break;
             }
         }
-        __threadfence();
         s_ok = ok;
     }
     __syncthreads();
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
             part[((size_t)k * G + b) * 2 + 1] = ai;
         }
     }
-    if (!grid_barrier(bar, G, ctrl)) return;
+    if (!grid_barrier(bar, G, 2 * J, ctrl)) return;
 
     // ---- phase B: h = sum of the partials (fixed order; tpv threads per value, a power of
     // two <= 32 so that each value's threads are consecutive lanes of one warp) --------------
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
             for (int q = 0; q < kFuseThreads / 32; ++q) t += red[q];
             part[(size_t)nv * G * 2 + b] = t;
         }
-        if (!grid_barrier(bar, G, ctrl)) return;
+        if (!grid_barrier(bar, G, 2 * J + 1, ctrl)) return;
     }
 
     // ---- phase C: Hessenberg column, beta and the breakdown test (CTA 0) --------------------
@@ -266,6 +268,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
     __shared__ float2 hf[kMaxBasis + 1], hl[kMaxBasis + 1];
     __shared__ double hs[2 * (kMaxBasis + 1)];
     __shared__ float2 red[kCgsWarps];
+    __shared__ __align__(8) unsigned long long s_bar;
     if (ctrl->broken) return;                        // uniform: written only between launches
     const int nv = J + 1, G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long i0 = (long)b * chunk;
@@ -273,8 +276,36 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
     float2* ws = reinterpret_cast<float2*>(smem_raw);
     float4* c0 = reinterpret_cast<float4*>(smem_raw + (((size_t)chunk * sizeof(float2) + 15) & ~(size_t)15));
     float2* cache = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(c0) + (v0s ? (size_t)chunk * 16 : 0));
-    for (int i = tid; i < cl; i += kFuseThreads) ws[i] = w[i0 + i];
-    __syncthreads();
+    // With the cache, the CTA's whole share (w, the first vector, every basis row) arrives by
+    // bulk asynchronous copies issued at once, so phase A waits one memory latency instead
+    // of one per unrolled load round.  Row starts are 16-byte aligned when n is even (chunk
+    // is a multiple of 8).
+    const bool tma = CACHE && (n & 1) == 0 && cl > 0;
+    const int k_first = v0s ? 1 : 0;                 // rows of V read (row 0 replaced by v0s)
+    if (tma) {
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&s_bar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned row = (unsigned)cl * 8;
+            const unsigned bytes = row * (unsigned)(1 + (v0s ? 2 : 0) + (nv - k_first));
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         :: "r"(smem_u32(&s_bar)), "r"(bytes) : "memory");
+            bulk_g2s(ws, w + i0, row, &s_bar);
+            if (v0s) bulk_g2s(c0, v0s + i0, 2 * row, &s_bar);
+            for (int k = k_first; k < nv; ++k) bulk_g2s(cache + (size_t)k * chunk, V + (size_t)k * n + i0, row, &s_bar);
+        }
+        if (!__syncthreads_and(mbar_wait0(&s_bar))) {
+            if (tid == 0) ctrl->wait_timeout = 1;
+            mbar_wait0(&s_bar);                      // copies in flight land before exit
+            return;
+        }
+    } else {
+        for (int i = tid; i < cl; i += kFuseThreads) ws[i] = w[i0 + i];
+        __syncthreads();
+    }
 
     // ---- phase A: partials of conj(v_k) . w; with fewer vectors than warps each vector's
     // chunk is cut into S slices (one warp each), summed in slice order afterwards
@@ -286,8 +317,8 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
         float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f, sh = 0.f, sl2 = 0.f, th = 0.f, tl = 0.f;
         if (v0s && k == 0) {
             for (int i = e0 + lane; i < e1; i += 32) {
-                const float4 a = v0s[i0 + i];
-                if (CACHE) c0[i] = a;
+                const float4 a = tma ? c0[i] : v0s[i0 + i];
+                if (CACHE && !tma) c0[i] = a;
                 const float2 x = ws[i];
                 // conj(a) x with a = hi + lo: re = ar xr + ai xi, im = ar xi - ai xr
                 acc_prod(rh, rl, a.x, a.z, x.x);
@@ -296,7 +327,8 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
                 acc_prod(th, tl, -a.y, -a.w, x.x);
             }
         } else {
-            const float2* vk = V + (size_t)k * n + i0;
+            const float2* vk = tma ? cache + (size_t)k * chunk : V + (size_t)k * n + i0;
+            const bool fill = CACHE && !tma;
             int i = e0 + lane;
             for (; i + 96 < e1; i += 128) {
                 float2 v[4];
@@ -304,7 +336,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
                 for (int u = 0; u < 4; ++u) v[u] = vk[i + 32 * u];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    if (CACHE) cache[(size_t)k * chunk + i + 32 * u] = v[u];
+                    if (fill) cache[(size_t)k * chunk + i + 32 * u] = v[u];
                     const float2 x = ws[i + 32 * u];
                     if (u & 1) {
                         acc_prod(sh, sl2, v[u].x, 0.f, x.x);
@@ -321,7 +353,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
             }
             for (; i < e1; i += 32) {
                 const float2 v = vk[i];
-                if (CACHE) cache[(size_t)k * chunk + i] = v;
+                if (fill) cache[(size_t)k * chunk + i] = v;
                 const float2 x = ws[i];
                 acc_prod(rh, rl, v.x, 0.f, x.x);
                 acc_prod(rh, rl, v.y, 0.f, x.y);
@@ -351,7 +383,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
             part[(size_t)tid * G + b] = a;
         }
     }
-    if (!grid_barrier(bar, G, ctrl)) return;
+    if (!grid_barrier(bar, G, 2 * J, ctrl)) return;
 
     // ---- phase B: h_k = sum over the CTAs' partials, every CTA in the same fixed order:
     // tpv consecutive lanes per vector, lane q taking partials q, q + tpv, ... (four loads in
@@ -362,22 +394,22 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
         const int k = tid / tpv, q = tid % tpv;
         float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
         if (k < nv) {
+            // all of a lane's partials in flight at once (12 per round covers G <= 12 tpv);
+            // zero padding leaves a compensated sum unchanged
+            constexpr int kRound = 12;
             const float4* p = part + (size_t)k * G;
-            int g = q;
-            for (; g + 3 * tpv < G; g += 4 * tpv) {
-                float4 c[4];
+            for (int g0 = q; g0 < G; g0 += kRound * tpv) {
+                float4 c[kRound];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) c[u] = __ldcg(p + g + u * tpv);
+                for (int u = 0; u < kRound; ++u) {
+                    const int g = g0 + u * tpv;
+                    c[u] = g < G ? __ldcg(p + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < kRound; ++u) {
                     acc_pair(rh, rl, c[u].x, c[u].y);
                     acc_pair(ih, il, c[u].z, c[u].w);
                 }
-            }
-            for (; g < G; g += tpv) {
-                const float4 c = __ldcg(p + g);
-                acc_pair(rh, rl, c.x, c.y);
-                acc_pair(ih, il, c.z, c.w);
             }
         }
         for (int o = 1; o < tpv; o <<= 1) {
@@ -443,7 +475,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
             for (int q = 0; q < kCgsWarps; ++q) acc_pair(a, c, red[q].x, red[q].y);
             part[(size_t)nv * G + b] = make_float4(a, c, 0.f, 0.f);
         }
-        if (!grid_barrier(bar, G, ctrl)) return;
+        if (!grid_barrier(bar, G, 2 * J + 1, ctrl)) return;
     }
 
     // ---- phase C: Hessenberg column, beta and the breakdown test (CTA 0) --------------------
@@ -451,9 +483,15 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
     __shared__ double s_beta;
     if (update && warp == 0) {
         float a = 0.f, c = 0.f;
-        for (int g = lane; g < G; g += 32) {
-            const float4 t = __ldcg(part + (size_t)nv * G + g);
-            acc_pair(a, c, t.x, t.y);
+        for (int g0 = lane; g0 < G; g0 += 8 * 32) {
+            float4 t[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int g = g0 + 32 * u;
+                t[u] = g < G ? __ldcg(part + (size_t)nv * G + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc_pair(a, c, t[u].x, t[u].y);
         }
         warp_pair_sum(a, c);
         if (lane == 0) s_beta = sqrt((double)a + (double)c);

@@ -80,6 +80,33 @@ __device__ __forceinline__ void set_inv_beta(Ctrl* c, double beta) {
     c->inv_beta_f[1] = (float)(ib - (double)h);
 }
 
+// ---------------------------------------------------------------------------
+// bulk asynchronous copies global -> shared, completed on an mbarrier
+// ---------------------------------------------------------------------------
+constexpr long kInvWaitLimit = 1L << 24;      // try_wait polls before a staging wait gives up
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+// Bounded wait for phase 0 of the mbarrier; false when the poll limit was reached.
+__device__ __forceinline__ bool mbar_wait0(unsigned long long* bar) {
+    const unsigned a = smem_u32(bar);
+    for (long it = 0; it < kInvWaitLimit; ++it) {
+        unsigned done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+                     " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(a) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // Programmatic dependent launch: a kernel launched with launch_pdl is scheduled as its
 // predecessor's CTAs retire (no explicit early trigger: CTAs of the next kernel waiting on
 // SMs slowed the solve measurably), hiding the launch gap between stream-launched kernels;

@@ -1273,16 +1273,22 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
     // throughput-heavy and they are split over the cluster by column.
     for (int k = tid; k < mm; k += blockDim.x) LU[k] = make_double2(Q[k].x - P[k].x, Q[k].y - P[k].y);   // D (FP64)
     __syncthreads();                                      // D is read below with another mapping
-    // Z = D^-1 in FP32 by Gauss-Jordan elimination with partial pivoting on |re|+|im|
-    // (all threads update the m x 2m block [D | I] at every pivot step)
-    float2* F = reinterpret_cast<float2*>(X);            // [D | I] rows of 2m float2 (m*2m float2)
+    // Z = D^-1 in FP32 by Gauss-Jordan elimination with partial pivoting on |re|+|im| on
+    // [D | I] (rows of 2m float2).  Each pivot step reads one buffer and writes the other
+    // (X and T, both free here): the row swap and the pivot-row scaling are folded into the
+    // update, out(r) = row'(r) - mult'(r) * newrow with row' the swapped rows, so a step
+    // costs two block barriers.  Columns <= k of the left half are finished and not written.
+    // The start buffer is chosen so that the last step writes X.
     const int w2 = 2 * m;
-    const float2* Z = F + m;                              // the inverse ends in the right half:
-                                                          // Z(r, k) = Z[r * w2 + k]
+    float2* Fr = reinterpret_cast<float2*>((m & 1) ? T : X);
+    float2* Fw = reinterpret_cast<float2*>((m & 1) ? X : T);
+    __shared__ float2 s_inv;
     for (int k = tid; k < m * w2; k += blockDim.x) {
         const int r = k / w2, c = k - r * w2;
-        F[k] = c < m ? make_float2((float)LU[r * m + c].x, (float)LU[r * m + c].y)
-                     : make_float2(c - m == r ? 1.f : 0.f, 0.f);
+        const float2 v = c < m ? make_float2((float)LU[r * m + c].x, (float)LU[r * m + c].y)
+                               : make_float2(c - m == r ? 1.f : 0.f, 0.f);
+        Fr[k] = v;
+        Fw[k] = v;
     }
     __syncthreads();
     for (int k = 0; k < m; ++k) {
@@ -1290,7 +1296,7 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
             float best = -1.f;
             int bi = k;
             for (int r = k + tid; r < m; r += 32) {
-                const float v = fabsf(F[r * w2 + k].x) + fabsf(F[r * w2 + k].y);
+                const float v = fabsf(Fr[r * w2 + k].x) + fabsf(Fr[r * w2 + k].y);
                 if (v > best) { best = v; bi = r; }
             }
             for (int o = 16; o > 0; o >>= 1) {
@@ -1301,43 +1307,37 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
             if (tid == 0) {
                 if (best == 0.f && !s_info) s_info = k + 1;
                 s_p = (best == 0.f) ? -1 : bi;
+                if (best != 0.f) {
+                    const float2 d = Fr[bi * w2 + k];
+                    const float den = d.x * d.x + d.y * d.y;
+                    s_inv = make_float2(d.x / den, -d.y / den);
+                }
             }
         }
         __syncthreads();
         const int p = s_p;
         if (p < 0) break;                                  // singular (uniform: s_p is shared)
-        // swap rows k and p, then scale row k by 1/pivot (one thread per column)
-        for (int c = tid; c < w2; c += blockDim.x) {
-            float2 a = F[k * w2 + c];
-            if (p != k) {
-                const float2 b = F[p * w2 + c];
-                F[p * w2 + c] = a;
-                a = b;
+        const float2 inv = s_inv;
+        const int nleft = m - k - 1, ncols = nleft + m;
+        const float2 fkk = Fr[k * w2 + k];                 // multiplier of the row that moves to p
+        for (int j = tid & 63; j < ncols; j += 64) {
+            const int c = j < nleft ? k + 1 + j : m + (j - nleft);
+            const float2 pr = Fr[p * w2 + c], rk = Fr[k * w2 + c];
+            const float2 nw = make_float2(pr.x * inv.x - pr.y * inv.y, pr.x * inv.y + pr.y * inv.x);
+            for (int r = tid >> 6; r < m; r += (int)(blockDim.x >> 6)) {
+                float2 out = nw;
+                if (r != k) {
+                    const float2 src = r == p ? rk : Fr[r * w2 + c];
+                    const float2 f = r == p ? fkk : Fr[r * w2 + k];
+                    out = make_float2(src.x - (f.x * nw.x - f.y * nw.y), src.y - (f.x * nw.y + f.y * nw.x));
+                }
+                Fw[r * w2 + c] = out;
             }
-            F[k * w2 + c] = a;
         }
         __syncthreads();
-        const float2 d = F[k * w2 + k];
-        const float den = d.x * d.x + d.y * d.y;
-        const float2 inv = make_float2(d.x / den, -d.y / den);
-        __syncthreads();
-        for (int c = tid; c < w2; c += blockDim.x) {
-            const float2 a = F[k * w2 + c];
-            F[k * w2 + c] = make_float2(a.x * inv.x - a.y * inv.y, a.x * inv.y + a.y * inv.x);
-        }
-        __syncthreads();
-        // eliminate column k from every other row
-        for (int idx = tid; idx < m * w2; idx += blockDim.x) {
-            const int r = idx / w2, c = idx - r * w2;
-            if (r == k || c <= k) continue;
-            const float2 fr = F[r * w2 + k], u = F[k * w2 + c];
-            float2 q = F[r * w2 + c];
-            q.x -= fr.x * u.x - fr.y * u.y;
-            q.y -= fr.x * u.y + fr.y * u.x;
-            F[r * w2 + c] = q;
-        }
-        __syncthreads();
+        float2* t = Fr; Fr = Fw; Fw = t;
     }
+    const float2* Z = reinterpret_cast<const float2*>(X) + m;   // the inverse: Z(r, k) = Z[r * w2 + k]
     const int info = s_info;
     if (info) {
         if (rank == 0 && tid == 0) ctrl->lu_info = info;

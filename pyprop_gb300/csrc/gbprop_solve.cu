@@ -370,29 +370,6 @@ cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, cons
 // slices of M and U~ arrive by bulk asynchronous copies (one mbarrier) while the threads
 // load the right-hand side.
 constexpr int kInvThreads = 512;
-constexpr long kInvWaitLimit = 1L << 24;      // try_wait polls before a staging wait gives up
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-    return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
-}
-
-// Bounded wait for phase 0 of the mbarrier; false when the poll limit was reached.
-__device__ __forceinline__ bool mbar_wait0(unsigned long long* bar) {
-    const unsigned a = smem_u32(bar);
-    for (long it = 0; it < kInvWaitLimit; ++it) {
-        unsigned done;
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
-                     " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(a) : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
 // x (+)= M r32 for element q: FP32 products, four independent chains per component.
 template <bool STAGE>
 __device__ __forceinline__ float2 inv_apply(const float* mrow, size_t mstride, const float2* r32, int q, int w) {
