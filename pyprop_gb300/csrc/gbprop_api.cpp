@@ -502,9 +502,15 @@ void set_inv_chunks(gbprop_ctx* h, bool wide) {
         InvTab& t = h->inv[dir];
         const int P = t.refine, w = t.w;
         auto chunk_of = [&](int nch) { return std::max(4, ((n + nch - 1) / nch + 3) & ~3); };
+        // the table serves the FP64-accurate solve and, on mixed handles, the complex64 basis
+        // solve (which also stages the FP32 pairs of U~): both must fit
+        const bool mixed = h->prec != GBPROP_FP64;
         auto smem_of = [&](int chunk, int stage) {
             size_t mx = 0;
-            for (int q0 = 0; q0 < n; q0 += chunk) mx = std::max(mx, inv_smem_bytes(n, q0, chunk, P, w, kd, stage, 1));
+            for (int q0 = 0; q0 < n; q0 += chunk) {
+                mx = std::max(mx, inv_smem_bytes(n, q0, chunk, P, w, kd, stage, 1));
+                if (mixed) mx = std::max(mx, inv_smem_bytes_mixed(n, q0, chunk, w, kd, stage));
+            }
             return mx;
         };
         // cost ~ (waves of resident CTAs) x (elements one CTA processes over all passes); CTAs

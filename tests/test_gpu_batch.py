@@ -72,3 +72,24 @@ def test_batch_mixed_precision_error_report():
         errs.append(rel(bp.psi[i].cpu().numpy().astype(np.complex128), want))
     print("FP32-mixed batch, 5 steps, relative L2 vs FP64 oracle per problem:", ["%.2e" % e for e in errs])
     assert max(errs) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
+def test_batch_long_radial_grid(precision):
+    """A radial grid long enough that one CTA cannot hold a whole row of the solve: the
+    chunking must fit both the FP64 solve and the complex64 basis solve."""
+    from pyprop_gb300 import _native
+    from pyprop_gb300.batch import BatchPropagator, HydrogenProblem
+    # radial sizes around where a whole row stops fitting one CTA (the complex64 solve also
+    # stages the FP32 pairs of U~, so its limit is lower than the FP64 solve's)
+    probs = [HydrogenProblem(lmax=1, nr=nr, rmax=0.5 * nr, m=8, omega=0.057, e0=0.05, dt=0.005, cycles=2, seed=7 + i)
+             for i, nr in enumerate((680, 720, 760, 800, 840, 1400))]
+    probs.append(HydrogenProblem(lmax=2, nr=60, rmax=50.0, m=6, omega=0.057, e0=0.05, dt=0.01, cycles=2, seed=3))
+    prec = _native.FP64 if precision == "fp64" else _native.FP32_MIXED
+    bp = BatchPropagator(probs, precision=prec, autotune=False)
+    psi0 = [p.initial_state() for p in probs]
+    bp.advance(2)
+    for i, p in enumerate(probs):
+        want, _ = _oracle(p).advance(psi0[i], p.m, p.dt, bp.scalings(i, 2))
+        err = rel(bp.psi[i].cpu().numpy().astype(np.complex128), want)
+        assert err < (1e-12 if precision == "fp64" else 1e-5), (i, err)
