@@ -15,7 +15,8 @@ PKG = os.path.dirname(HERE)
 ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbprop.so")
-SOURCES = ["gbprop_kernels.cu", "gbprop_solve.cu", "gbprop_cgs.cu", "gbprop_api.cpp", "gbprop_noalloc.cu"]
+SOURCES = ["gbprop_kernels.cu", "gbprop_solve.cu", "gbprop_cgs.cu", "gbprop_expm.cu", "gbprop_api.cpp",
+           "gbprop_noalloc.cu"]
 HEADERS = ["gbprop_internal.h", "gbprop_device.cuh", os.path.join(ROOT, "include", "gbprop.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -654,7 +654,7 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
     const long N = h->N;
     char* V = (char*)h->d_V;
     if (gbprop_status st = enqueue_arnoldi(h, h->double_orth, std::sqrt(DBL_EPSILON))) return st;   // pamp.h:79
-    GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s));
+    GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s, h->prec != GBPROP_FP64));
     // x <- beta0 V exp(-i dt H) e1
     GB_LAUNCH(launch_combine(kp, V, h->d_v0, N, h->d_ctrl, h->d_x, s));
     GB_LAUNCH(launch_step_end(h->d_ctrl, s));

@@ -107,6 +107,78 @@ __device__ __forceinline__ bool mbar_wait0(unsigned long long* bar) {
     return false;
 }
 
+// FP32 Gauss-Jordan inverse of the m x m complex matrix D = dval(r, c) (float2) with partial
+// pivoting on |re|+|im| (first maximum) on [D | I], rows of 2m float2.  The row swap and the
+// pivot-row scaling are folded into the update, out(r) = row'(r) - mult'(r) * newrow with row' the
+// swapped rows, so a pivot step reads one buffer and writes the other and costs two block
+// barriers; finished left columns (<= k) are not written.  Fa is read first; the result ends in Fa
+// when m is even, in Fb when m is odd, as the right half (row stride 2m).  Returns 0, or the
+// 1-based column of the first zero pivot (then the buffers hold no inverse).  Whole block.
+template <typename DV>
+__device__ int gj_inverse_f32(int m, DV dval, float2* Fa, float2* Fb) {
+    __shared__ int s_piv;
+    __shared__ float2 s_inv;
+    const int tid = threadIdx.x, w2 = 2 * m;
+    for (int k = tid; k < m * w2; k += blockDim.x) {
+        const int r = k / w2, c = k - r * w2;
+        const float2 v = c < m ? dval(r, c) : make_float2(c - m == r ? 1.f : 0.f, 0.f);
+        Fa[k] = v;
+        Fb[k] = v;
+    }
+    __syncthreads();
+    float2* Fr = Fa;
+    float2* Fw = Fb;
+    int info = 0;
+    for (int k = 0; k < m; ++k) {
+        if (tid < 32) {
+            float best = -1.f;
+            int bi = k;
+            for (int r = k + tid; r < m; r += 32) {
+                const float v = fabsf(Fr[r * w2 + k].x) + fabsf(Fr[r * w2 + k].y);
+                if (v > best) { best = v; bi = r; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (tid == 0) {
+                s_piv = (best == 0.f) ? -1 : bi;
+                if (best != 0.f) {
+                    const float2 d = Fr[bi * w2 + k];
+                    const float den = d.x * d.x + d.y * d.y;
+                    s_inv = make_float2(d.x / den, -d.y / den);
+                }
+            }
+        }
+        __syncthreads();
+        const int p = s_piv;
+        if (p < 0) { info = k + 1; break; }           // singular (uniform: s_piv is shared)
+        const float2 inv = s_inv;
+        const int nleft = m - k - 1, ncols = nleft + m;
+        const float2 fkk = Fr[k * w2 + k];             // multiplier of the row that moves to p
+        for (int j = tid & 63; j < ncols; j += 64) {
+            const int c = j < nleft ? k + 1 + j : m + (j - nleft);
+            const float2 pr = Fr[p * w2 + c], rk = Fr[k * w2 + c];
+            const float2 nw = make_float2(pr.x * inv.x - pr.y * inv.y, pr.x * inv.y + pr.y * inv.x);
+            for (int r = tid >> 6; r < m; r += (int)(blockDim.x >> 6)) {
+                float2 out = nw;
+                if (r != k) {
+                    const float2 src = r == p ? rk : Fr[r * w2 + c];
+                    const float2 f = r == p ? fkk : Fr[r * w2 + k];
+                    out = make_float2(src.x - (f.x * nw.x - f.y * nw.y), src.y - (f.x * nw.y + f.y * nw.x));
+                }
+                Fw[r * w2 + c] = out;
+            }
+        }
+        __syncthreads();
+        float2* t = Fr;
+        Fr = Fw;
+        Fw = t;
+    }
+    return info;
+}
+
 // Programmatic dependent launch: a kernel launched with launch_pdl is scheduled as its
 // predecessor's CTAs retire (no explicit early trigger: CTAs of the next kernel waiting on
 // SMs slowed the solve measurably), hiding the launch gap between stream-launched kernels;

@@ -211,7 +211,10 @@ inline size_t arnoldi_cgs_part_doubles(int grid) { return (size_t)(2 * (kMaxBasi
 cudaError_t launch_step_begin(Ctrl* ctrl, double* H, int m, cudaStream_t s);
 // max_cluster: 16 lets one problem's exponential spread over a thread-block cluster; 1 keeps it on
 // one CTA (batches, where other problems fill the GPU).
-cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s);
+// df32 = 1 (FP32-mixed handles): the cluster form in double-float arithmetic (gbprop_expm.cu).
+cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s,
+                        int df32 = 0);
+cudaError_t launch_expm_df(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int cluster, cudaStream_t s);
 cudaError_t launch_combine(int prec, const void* V, const double2* v0, long n, const Ctrl* ctrl, void* out,
                            cudaStream_t s);
 cudaError_t launch_step_end(Ctrl* ctrl, cudaStream_t s);

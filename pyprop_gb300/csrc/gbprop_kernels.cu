@@ -1273,70 +1273,16 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
     // throughput-heavy and they are split over the cluster by column.
     for (int k = tid; k < mm; k += blockDim.x) LU[k] = make_double2(Q[k].x - P[k].x, Q[k].y - P[k].y);   // D (FP64)
     __syncthreads();                                      // D is read below with another mapping
-    // Z = D^-1 in FP32 by Gauss-Jordan elimination with partial pivoting on |re|+|im| on
-    // [D | I] (rows of 2m float2).  Each pivot step reads one buffer and writes the other
-    // (X and T, both free here): the row swap and the pivot-row scaling are folded into the
-    // update, out(r) = row'(r) - mult'(r) * newrow with row' the swapped rows, so a step
-    // costs two block barriers.  Columns <= k of the left half are finished and not written.
-    // The start buffer is chosen so that the last step writes X.
+    // Z = D^-1 in FP32 (Gauss-Jordan, see gj_inverse_f32); X and T are free here, the start
+    // buffer is chosen so that the result lands in X
     const int w2 = 2 * m;
-    float2* Fr = reinterpret_cast<float2*>((m & 1) ? T : X);
-    float2* Fw = reinterpret_cast<float2*>((m & 1) ? X : T);
-    __shared__ float2 s_inv;
-    for (int k = tid; k < m * w2; k += blockDim.x) {
-        const int r = k / w2, c = k - r * w2;
-        const float2 v = c < m ? make_float2((float)LU[r * m + c].x, (float)LU[r * m + c].y)
-                               : make_float2(c - m == r ? 1.f : 0.f, 0.f);
-        Fr[k] = v;
-        Fw[k] = v;
+    {
+        const int gi = gj_inverse_f32(
+            m, [&](int r, int c) { return make_float2((float)LU[r * m + c].x, (float)LU[r * m + c].y); },
+            reinterpret_cast<float2*>((m & 1) ? T : X), reinterpret_cast<float2*>((m & 1) ? X : T));
+        if (tid == 0 && gi && !s_info) s_info = gi;
     }
     __syncthreads();
-    for (int k = 0; k < m; ++k) {
-        if (tid < 32) {
-            float best = -1.f;
-            int bi = k;
-            for (int r = k + tid; r < m; r += 32) {
-                const float v = fabsf(Fr[r * w2 + k].x) + fabsf(Fr[r * w2 + k].y);
-                if (v > best) { best = v; bi = r; }
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-            }
-            if (tid == 0) {
-                if (best == 0.f && !s_info) s_info = k + 1;
-                s_p = (best == 0.f) ? -1 : bi;
-                if (best != 0.f) {
-                    const float2 d = Fr[bi * w2 + k];
-                    const float den = d.x * d.x + d.y * d.y;
-                    s_inv = make_float2(d.x / den, -d.y / den);
-                }
-            }
-        }
-        __syncthreads();
-        const int p = s_p;
-        if (p < 0) break;                                  // singular (uniform: s_p is shared)
-        const float2 inv = s_inv;
-        const int nleft = m - k - 1, ncols = nleft + m;
-        const float2 fkk = Fr[k * w2 + k];                 // multiplier of the row that moves to p
-        for (int j = tid & 63; j < ncols; j += 64) {
-            const int c = j < nleft ? k + 1 + j : m + (j - nleft);
-            const float2 pr = Fr[p * w2 + c], rk = Fr[k * w2 + c];
-            const float2 nw = make_float2(pr.x * inv.x - pr.y * inv.y, pr.x * inv.y + pr.y * inv.x);
-            for (int r = tid >> 6; r < m; r += (int)(blockDim.x >> 6)) {
-                float2 out = nw;
-                if (r != k) {
-                    const float2 src = r == p ? rk : Fr[r * w2 + c];
-                    const float2 f = r == p ? fkk : Fr[r * w2 + k];
-                    out = make_float2(src.x - (f.x * nw.x - f.y * nw.y), src.y - (f.x * nw.y + f.y * nw.x));
-                }
-                Fw[r * w2 + c] = out;
-            }
-        }
-        __syncthreads();
-        float2* t = Fr; Fr = Fw; Fw = t;
-    }
     const float2* Z = reinterpret_cast<const float2*>(X) + m;   // the inverse: Z(r, k) = Z[r * w2 + k]
     const int info = s_info;
     if (info) {
@@ -1490,9 +1436,11 @@ int expm_cluster_size(int m) {
     return g_expm_cluster[m] == 1 ? 0 : g_expm_cluster[m];
 }
 
-cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s) {
+cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s,
+                        int df32) {
     count_launch();
     const int cl = max_cluster >= 8 ? expm_cluster_size(m) : 0;
+    if (df32 && (cl == 16 || cl == 8) && cl <= max_cluster) return launch_expm_df(ctrl, H, m, sched, cl, s);
     if (cl == 16 && max_cluster >= 16) return launch_expm_cl<16>(ctrl, H, m, sched, s);
     if (cl == 8) return launch_expm_cl<8>(ctrl, H, m, sched, s);
     const size_t smem = (size_t)5 * m * m * sizeof(double2);
