@@ -550,10 +550,11 @@ void set_inv_chunks(gbprop_ctx* h, bool wide) {
 // Triangular solve of the Krylov precision: FP64-accurate (FP32 solve + FP64 refinement)
 // for the FP64 path, plain complex64 for the mixed path's basis.
 cudaError_t ksolve(gbprop_ctx* h, int dir, const void* in, int in_prec, void* out, int out_prec, void* vstore,
-                   int v_prec, int scale_mode, int check_broken, float4* v0s = nullptr) {
+                   int v_prec, int scale_mode, int check_broken, float4* v0s = nullptr, const void* bpart = nullptr) {
     if (h->inv_ok)
         return launch_solve_inv(h->inv[dir], h->nl, h->prec == GBPROP_FP64 ? 1 : 0, in, in_prec, out, out_prec,
-                                vstore, v_prec, h->d_ctrl, dir, scale_mode, check_broken, h->stream, v0s);
+                                vstore, v_prec, h->d_ctrl, dir, scale_mode, check_broken, h->stream, v0s, bpart,
+                                h->cgs_grid);
     if (h->prec == GBPROP_FP64)
         return launch_solve_ir(&h->t32.tab[dir], h->d_ud_phys, h->nl, in, in_prec, out, out_prec, vstore, v_prec,
                                h->d_ctrl, scale_mode, check_broken, h->stream);
@@ -605,8 +606,9 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
     char* V = (char*)h->d_V;
     const size_t vbytes = (size_t)N * h->kelem();
     GB_LAUNCH(launch_step_begin(h->d_ctrl, h->d_H, m, s));
-    // the complex64 form reads the split first vector, which only the inverse-band solve writes
-    const bool fused = h->cgs_grid > 0 && !dorth && h->expm_max_cluster > 1 && (h->prec == GBPROP_FP64 || h->inv_ok);
+    // the fused form hands beta to the next solve and (complex64) reads the split first vector:
+    // both only the inverse-band solve provides
+    const bool fused = h->cgs_grid > 0 && !dorth && h->expm_max_cluster > 1 && h->inv_ok;
     if (fused) GB_CUDA(cudaMemsetAsync(h->d_gridbar, 0, 2 * sizeof(unsigned), s));
     // beta0 = ||x||
     GB_LAUNCH(launch_norm(0, h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
@@ -614,10 +616,15 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
         const void* in = J == 0 ? (const void*)h->d_x : (const void*)h->d_r;
         const int in_prec = J == 0 ? 0 : kp;
         // v_J = r / beta_J stored in V[J] (v_0 of a complex64 basis in FP64); s = U^-1 v_J
+        // fused: beta_J comes from the previous Gram-Schmidt launch's ||w||^2 partials (see
+        // launch_solve_inv); they follow that launch's J inner-product partials, 16 bytes per
+        // (vector, CTA) in both forms (two doubles, or one float4 of FP32 pairs)
+        const void* bpart = nullptr;
+        if (fused && J > 0) bpart = (const char*)h->d_cgs_part + (size_t)J * h->cgs_grid * 16;
         if (J == 0 && h->d_v0)
             GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, h->d_v0, 0, 1, 1, fused ? h->d_v0s : nullptr));
         else
-            GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1));
+            GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1, nullptr, bpart));
         // y = sum_t c_t s_t A_t s
         GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, h->d_sched, h->d_ctrl, 0.0, 1, s));
         // w = U^-T y

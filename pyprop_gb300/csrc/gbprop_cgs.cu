@@ -6,8 +6,9 @@
 // element chunk [b*C, (b+1)*C) of every basis vector: it reads its chunk of V once into
 // shared memory (when it fits), forms its partial inner products, and after a grid
 // barrier every CTA sums all CTAs' partials in the same fixed order (deterministic, the
-// same h everywhere), updates its chunk of w from the cached V and contributes ||w||^2;
-// after a second barrier CTA 0 writes the Hessenberg column and the control block.
+// same h everywhere), updates its chunk of w from the cached V and writes its share of
+// ||w||^2; CTA 0 writes the Hessenberg column and the counters.  beta = ||w|| is formed from
+// those shares by the next solve, the first kernel that needs it (see launch_solve_inv).
 // Versus separate dot / update / finalize kernels this reads V once instead of twice and
 // removes two launches and two last-block reductions per Arnoldi step.
 #include "gbprop_internal.h"
@@ -60,6 +61,30 @@ __device__ __forceinline__ void acc_dot64(double& ar, double& ai, double vr, dou
     ar = fma(vi, xi, ar);
     ai = fma(vr, xi, ai);
     ai = fma(-vi, xr, ai);
+}
+
+// Phase C (CTA 0): the Hessenberg column J and the counters (pamp.h:305-345).  beta of the next
+// vector, its breakdown test and 1/beta are formed from the ||w||^2 partials by the next solve
+// (the first kernel that needs them), which saves a grid barrier here; H(J, J-1) = beta_J,
+// recorded by the solve of this Arnoldi step, is written now.
+__device__ __forceinline__ void cgs_finish(Ctrl* ctrl, double* H, const double* hs, int m, int J, int b) {
+    if (b != 0) return;
+    const int nv = J + 1;
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+        H[2 * ((size_t)k * m + J)] = hs[2 * k];
+        H[2 * ((size_t)k * m + J) + 1] = hs[2 * k + 1];
+        ctrl->h[2 * k] = hs[2 * k];
+        ctrl->h[2 * k + 1] = hs[2 * k + 1];
+    }
+    if (threadIdx.x == 0) {
+        ctrl->nbasis = nv;
+        ctrl->operator_count++;
+        if (J == 0) ctrl->inner_product_count++;
+        if (J > 0) {
+            H[2 * ((size_t)J * m + J - 1)] = ctrl->beta;
+            H[2 * ((size_t)J * m + J - 1) + 1] = 0.0;
+        }
+    }
 }
 
 template <bool CACHE>
@@ -128,7 +153,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
             part[((size_t)k * G + b) * 2 + 1] = ai;
         }
     }
-    if (!grid_barrier(bar, G, 2 * J, ctrl)) return;
+    if (!grid_barrier(bar, G, J, ctrl)) return;   // the launch's only barrier: number J of the step
 
     // ---- phase B: h = sum of the partials (fixed order; tpv threads per value, a power of
     // two <= 32 so that each value's threads are consecutive lanes of one warp) --------------
@@ -193,48 +218,10 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
         if (tid == 0) {
             double t = 0.0;
             for (int q = 0; q < kFuseThreads / 32; ++q) t += red[q];
-            part[(size_t)nv * G * 2 + b] = t;
-        }
-        if (!grid_barrier(bar, G, 2 * J + 1, ctrl)) return;
-    }
-
-    // ---- phase C: Hessenberg column, beta and the breakdown test (CTA 0) --------------------
-    if (b != 0) return;
-    __shared__ double s_beta;
-    if (update && warp == 0) {
-        double t = 0.0;
-        for (int g = lane; g < G; g += 32) t += __ldcg(part + (size_t)nv * G * 2 + g);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) s_beta = sqrt(t);
-    }
-    __syncthreads();
-    for (int k = tid; k < nv; k += kFuseThreads) {
-        H[2 * ((size_t)k * m + J)] = hs[2 * k];
-        H[2 * ((size_t)k * m + J) + 1] = hs[2 * k + 1];
-        ctrl->h[2 * k] = hs[2 * k];
-        ctrl->h[2 * k + 1] = hs[2 * k + 1];
-    }
-    if (tid == 0) {
-        ctrl->nbasis = nv;
-        ctrl->operator_count++;
-        if (J == 0) ctrl->inner_product_count++;
-        if (J + 1 < m) {
-            const double beta = s_beta;
-            ctrl->resid_norm = beta;
-            const double tol = sqrt(DBL_EPSILON);   // pamp.h:79
-            if (!isfinite(beta)) ctrl->nonfinite = 1;
-            if (fabs(beta) < tol) {
-                ctrl->broken = 1;
-                ctrl->breakdown_count++;
-            } else {
-                H[2 * ((size_t)(J + 1) * m + J)] = beta;
-                H[2 * ((size_t)(J + 1) * m + J) + 1] = 0.0;
-                ctrl->beta = beta;
-                set_inv_beta(ctrl, beta);
-            }
+            part[(size_t)nv * G * 2 + b] = t;     // beta is formed from these by the next solve
         }
     }
+    cgs_finish(ctrl, H, hs, m, J, b);
 }
 
 // ---------------------------------------------------------------------------
@@ -247,15 +234,6 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
 // threads touch FP64 (the Hessenberg entries, beta).
 constexpr int kCgsWarps = kFuseThreads / 32;
 constexpr int kCgsItems = 64;
-
-// compensated butterfly over the warp: every lane ends with the same (hi, lo)
-__device__ __forceinline__ void warp_pair_sum(float& h, float& l) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
-        acc_pair(h, l, oh, ol);
-    }
-}
 
 template <bool CACHE>
 __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __restrict__ V,
@@ -383,7 +361,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
             part[(size_t)tid * G + b] = a;
         }
     }
-    if (!grid_barrier(bar, G, 2 * J, ctrl)) return;
+    if (!grid_barrier(bar, G, J, ctrl)) return;   // the launch's only barrier: number J of the step
 
     // ---- phase B: h_k = sum over the CTAs' partials, every CTA in the same fixed order:
     // tpv consecutive lanes per vector, lane q taking partials q, q + tpv, ... (four loads in
@@ -473,56 +451,10 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
         if (tid == 0) {
             float a = 0.f, c = 0.f;
             for (int q = 0; q < kCgsWarps; ++q) acc_pair(a, c, red[q].x, red[q].y);
-            part[(size_t)nv * G + b] = make_float4(a, c, 0.f, 0.f);
-        }
-        if (!grid_barrier(bar, G, 2 * J + 1, ctrl)) return;
-    }
-
-    // ---- phase C: Hessenberg column, beta and the breakdown test (CTA 0) --------------------
-    if (b != 0) return;
-    __shared__ double s_beta;
-    if (update && warp == 0) {
-        float a = 0.f, c = 0.f;
-        for (int g0 = lane; g0 < G; g0 += 8 * 32) {
-            float4 t[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int g = g0 + 32 * u;
-                t[u] = g < G ? __ldcg(part + (size_t)nv * G + g) : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) acc_pair(a, c, t[u].x, t[u].y);
-        }
-        warp_pair_sum(a, c);
-        if (lane == 0) s_beta = sqrt((double)a + (double)c);
-    }
-    __syncthreads();
-    for (int k = tid; k < nv; k += kFuseThreads) {
-        H[2 * ((size_t)k * m + J)] = hs[2 * k];
-        H[2 * ((size_t)k * m + J) + 1] = hs[2 * k + 1];
-        ctrl->h[2 * k] = hs[2 * k];
-        ctrl->h[2 * k + 1] = hs[2 * k + 1];
-    }
-    if (tid == 0) {
-        ctrl->nbasis = nv;
-        ctrl->operator_count++;
-        if (J == 0) ctrl->inner_product_count++;
-        if (J + 1 < m) {
-            const double beta = s_beta;
-            ctrl->resid_norm = beta;
-            const double tol = sqrt(DBL_EPSILON);   // pamp.h:79
-            if (!isfinite(beta)) ctrl->nonfinite = 1;
-            if (fabs(beta) < tol) {
-                ctrl->broken = 1;
-                ctrl->breakdown_count++;
-            } else {
-                H[2 * ((size_t)(J + 1) * m + J)] = beta;
-                H[2 * ((size_t)(J + 1) * m + J) + 1] = 0.0;
-                ctrl->beta = beta;
-                set_inv_beta(ctrl, beta);
-            }
+            part[(size_t)nv * G + b] = make_float4(a, c, 0.f, 0.f);   // for the next solve's beta
         }
     }
+    cgs_finish(ctrl, H, hs, m, J, b);
 }
 
 size_t arnoldi_cgs_smem(int prec, long n, int nv, int grid, int with_v0, int cache) {

@@ -2,6 +2,7 @@
 #pragma once
 #include "gbprop_internal.h"
 
+#include <cfloat>
 #include <mutex>
 #include <unordered_set>
 
@@ -55,6 +56,16 @@ __device__ __forceinline__ void acc_scaled(float& hi, float& lo, float ch, float
     float t;
     two_sum(hi, p, hi, t);
     lo = __fadd_rn(lo, __fadd_rn(t, __fadd_rn(pe, __fmaf_rn(ch, sl, __fmul_rn(cl, sh)))));
+}
+
+// (h, l) += (ah + al)(bh + bl): exact ah*bh, cross terms to first order, error-free sum
+__device__ __forceinline__ void df_mac(float& h, float& l, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    const float e = __fmaf_rn(ah, bh, -p);
+    const float lo = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+    float t;
+    two_sum(h, p, h, t);
+    l = __fadd_rn(l, __fadd_rn(t, lo));
 }
 
 // (hi, lo) += (bh + bl)
@@ -177,6 +188,65 @@ __device__ int gj_inverse_f32(int m, DV dval, float2* Fa, float2* Fb) {
         Fw = t;
     }
     return info;
+}
+
+// compensated butterfly over the warp: every lane ends with the same (hi, lo)
+__device__ __forceinline__ void warp_pair_sum(float& h, float& l) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+        acc_pair(h, l, oh, ol);
+    }
+}
+
+// beta = ||w|| of the next basis vector from the cooperative Gram-Schmidt kernel's per-CTA
+// ||w||^2 partials, summed by one warp in a fixed order (the same beta in every CTA that
+// calls it).  PAIRS: FP32-pair partials (float4 hi, lo, -, -) of the complex64 form, else one
+// double per CTA.  Whole warp; returns beta in every lane.
+template <bool PAIRS>
+__device__ __forceinline__ double gs_beta(const void* part, int G) {
+    const int lane = threadIdx.x & 31;
+    if constexpr (PAIRS) {
+        const float4* p = reinterpret_cast<const float4*>(part);
+        float a = 0.f, c = 0.f;
+        for (int g0 = lane; g0 < G; g0 += 8 * 32) {
+            float4 t[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int g = g0 + 32 * u;
+                t[u] = g < G ? __ldcg(p + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc_pair(a, c, t[u].x, t[u].y);
+        }
+        warp_pair_sum(a, c);
+        return sqrt((double)a + (double)c);
+    } else {
+        const double* p = reinterpret_cast<const double*>(part);
+        double t = 0.0;
+        for (int g = lane; g < G; g += 32) t += __ldcg(p + g);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        return sqrt(t);
+    }
+}
+
+// Records beta of the next basis vector (pamp.h:330-345; happy breakdown below sqrt(eps),
+// pamp.h:79) in the control block when `writer`; returns true on breakdown.
+__device__ __forceinline__ bool gs_record_beta(Ctrl* ctrl, double beta, bool writer) {
+    const bool brk = fabs(beta) < sqrt(DBL_EPSILON);
+    if (writer) {
+        ctrl->resid_norm = beta;
+        if (!isfinite(beta)) ctrl->nonfinite = 1;
+        if (brk) {
+            ctrl->broken = 1;
+            ctrl->breakdown_count++;
+        } else {
+            ctrl->beta = beta;
+            set_inv_beta(ctrl, beta);
+        }
+    }
+    return brk;
 }
 
 // Programmatic dependent launch: a kernel launched with launch_pdl is scheduled as its

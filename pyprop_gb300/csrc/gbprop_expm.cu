@@ -34,16 +34,6 @@ __device__ __forceinline__ float4 df_of(double re, double im) {
     return make_float4(a, (float)(re - (double)a), b, (float)(im - (double)b));
 }
 
-// (h, l) += (ah + al)(bh + bl): exact ah*bh, cross terms to first order, error-free sum
-__device__ __forceinline__ void df_mac(float& h, float& l, float ah, float al, float bh, float bl) {
-    const float p = __fmul_rn(ah, bh);
-    const float e = __fmaf_rn(ah, bh, -p);
-    const float lo = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
-    float t;
-    two_sum(h, p, h, t);
-    l = __fadd_rn(l, __fadd_rn(t, lo));
-}
-
 __device__ __forceinline__ float4 df_normal(float rh, float rl, float ih, float il) {
     float a, b, c, d;
     two_sum(rh, rl, a, b);

@@ -171,10 +171,14 @@ cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, cons
 // path's Krylov basis: one refinement whose residual is formed with error-free FP32 products
 // and sums, complex64 output.  Grid: (tab.nchunks, nrows); arguments as launch_solve.
 // v0s (complex64 solve of the FP64 first vector only, may be null) receives the scaled input
-// split into FP32 pairs, float4 (re_hi, im_hi, re_lo, im_lo) per element.
+// split into FP32 pairs, float4 (re_hi, im_hi, re_lo, im_lo) per element.  bpart (scale_mode
+// 1, may be null): the cooperative Gram-Schmidt kernel's bG per-CTA ||w||^2 partials (double,
+// or float4 FP32 pairs for refine64 = 0); the solve forms beta from them, records it in ctrl
+// (breakdown test, 1/beta) and scales by 1/beta, instead of reading ctrl->inv_beta.
 cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
                              int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
-                             int check_broken, cudaStream_t s, float4* v0s = nullptr);
+                             int check_broken, cudaStream_t s, float4* v0s = nullptr, const void* bpart = nullptr,
+                             int bG = 0);
 cudaError_t launch_band_apply(int arith, const void* op, const void* x, void* y, const SchedEntry* sched,
                               const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s);
 cudaError_t launch_tbmv(int arith, int kd, const void* ud_phys, int nl, int nr, const void* in, int in_prec,

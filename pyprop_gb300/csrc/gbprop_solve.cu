@@ -406,7 +406,8 @@ template <int KD, bool R64, bool STAGE, typename TI, typename TO, typename TV>
 __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI* __restrict__ in,
                                                            TO* __restrict__ out, TV* __restrict__ vstore,
                                                            Ctrl* __restrict__ ctrl, int dir, int scale_mode,
-                                                           int check_broken) {
+                                                           int check_broken, const double* __restrict__ bpart,
+                                                           int bG) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ unsigned s_red[kInvThreads / 32];
     __shared__ __align__(8) unsigned long long s_bar;
@@ -462,18 +463,47 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
     const float* uhb = Uhg;
     const float* ulb = Ulg;
     const size_t ustride = (size_t)tab.npad;
-    const double sc = scale_mode ? ctrl->inv_beta : 1.0;
     const size_t base = (size_t)l * n;
 
     {
-        for (int q = tid; q < RB; q += kInvThreads) {
-            const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-            const TI t = in[base + p];
-            double2 b = make_double2((double)t.x, (double)t.y);
-            if (scale_mode) { b.x *= sc; b.y *= sc; }
-            if (vstore && q < cl) vstore[base + p] = conv<TV>(b);
-            bq[q] = b;
-            if (q < R0) xq[q] = make_double2(0.0, 0.0);
+        // late: 1/beta comes from the Gram-Schmidt kernel's norm partials -- warp 0 forms it
+        // while the other warps load the right-hand side, which is scaled afterwards
+        const bool late = scale_mode && bpart;
+        const double sc = scale_mode && !late ? ctrl->inv_beta : 1.0;
+        __shared__ double s_ibeta;
+        __shared__ int s_brk;
+        if (late && warp == 0) {
+            const double beta = gs_beta<false>(bpart, bG);
+            if (lane == 0) {
+                s_brk = gs_record_beta(ctrl, beta, blockIdx.x == 0 && blockIdx.y == 0);
+                s_ibeta = 1.0 / beta;
+            }
+        }
+        const int t0 = late ? tid - 32 : tid, tstep = late ? kInvThreads - 32 : kInvThreads;
+        if (t0 >= 0)
+            for (int q = t0; q < RB; q += tstep) {
+                const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+                const TI t = in[base + p];
+                double2 b = make_double2((double)t.x, (double)t.y);
+                if (scale_mode && !late) { b.x *= sc; b.y *= sc; }
+                if (vstore && q < cl && !late) vstore[base + p] = conv<TV>(b);
+                bq[q] = b;
+                if (q < R0) xq[q] = make_double2(0.0, 0.0);
+            }
+        if (late) {
+            __syncthreads();
+            if (s_brk) {                               // uniform: the same beta in every CTA
+                if (STAGE) mbar_wait0(&s_bar);
+                return;
+            }
+            const double ib = s_ibeta;
+            for (int q = tid; q < RB; q += kInvThreads) {
+                double2 b = bq[q];
+                b.x *= ib;
+                b.y *= ib;
+                bq[q] = b;
+                if (vstore && q < cl) vstore[base + (dir ? (n - 1 - (q0 + q)) : (q0 + q))] = conv<TV>(b);
+            }
         }
         bool ok = true;
         if (STAGE) ok = mbar_wait0(&s_bar);
@@ -602,7 +632,8 @@ template <int KD, bool STAGE, typename TI, typename TV>
 __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const TI* __restrict__ in,
                                                              float2* __restrict__ out, TV* __restrict__ vstore,
                                                              Ctrl* __restrict__ ctrl, int dir, int scale_mode,
-                                                             int check_broken, float4* __restrict__ v0s) {
+                                                             int check_broken, float4* __restrict__ v0s,
+                                                             const float4* __restrict__ bpart, int bG) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long s_bar;
     const int n = tab.n, w = tab.w;
@@ -677,20 +708,52 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
         }
     } else {
         // a complex64 vector: scaled by 1/beta as an FP32 pair, rounded once (no FP64
-        // instruction per element)
-        const float sh = scale_mode ? ctrl->inv_beta_f[0] : 1.f, sl = scale_mode ? ctrl->inv_beta_f[1] : 0.f;
-        for (int q = tid; q < R0 + w; q += kInvThreads) {
-            float2 hi = make_float2(0.f, 0.f);
-            if (q < RB) {
-                const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-                const TI t = in[base + p];
-                hi = make_float2((float)t.x, (float)t.y);
-                if (scale_mode) hi = make_float2(mul_pair(hi.x, sh, sl), mul_pair(hi.y, sh, sl));
-                if (vstore && q < cl) vstore[base + p] = conv<TV>(hi);
-                bh[q] = hi;
-                bl[q] = make_float2(0.f, 0.f);
+        // instruction per element).  late: 1/beta from the Gram-Schmidt kernel's norm
+        // partials, formed by warp 0 while the other warps load (see k_solve_inv)
+        const bool late = scale_mode && bpart;
+        __shared__ float2 s_ibf;
+        __shared__ int s_brk;
+        if (late && (tid >> 5) == 0) {
+            const double beta = gs_beta<true>(bpart, bG);
+            if ((tid & 31) == 0) {
+                s_brk = gs_record_beta(ctrl, beta, blockIdx.x == 0 && blockIdx.y == 0);
+                const double ib = 1.0 / beta;
+                const float h = (float)ib;
+                s_ibf = make_float2(h, (float)(ib - (double)h));
             }
-            r32[q] = hi;
+        }
+        float sh = 1.f, sl = 0.f;
+        if (scale_mode && !late) { sh = ctrl->inv_beta_f[0]; sl = ctrl->inv_beta_f[1]; }
+        const int t0 = late ? tid - 32 : tid, tstep = late ? kInvThreads - 32 : kInvThreads;
+        if (t0 >= 0)
+            for (int q = t0; q < R0 + w; q += tstep) {
+                float2 hi = make_float2(0.f, 0.f);
+                if (q < RB) {
+                    const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
+                    const TI t = in[base + p];
+                    hi = make_float2((float)t.x, (float)t.y);
+                    if (scale_mode && !late) hi = make_float2(mul_pair(hi.x, sh, sl), mul_pair(hi.y, sh, sl));
+                    if (vstore && q < cl && !late) vstore[base + p] = conv<TV>(hi);
+                    bh[q] = hi;
+                    bl[q] = make_float2(0.f, 0.f);
+                }
+                r32[q] = hi;
+            }
+        if (late) {
+            __syncthreads();
+            if (s_brk) {                               // uniform: the same beta in every CTA
+                if (STAGE) mbar_wait0(&s_bar);
+                return;
+            }
+            sh = s_ibf.x;
+            sl = s_ibf.y;
+            for (int q = tid; q < RB; q += kInvThreads) {
+                const float2 b = bh[q];
+                const float2 hi = make_float2(mul_pair(b.x, sh, sl), mul_pair(b.y, sh, sl));
+                bh[q] = hi;
+                r32[q] = hi;
+                if (vstore && q < cl) vstore[base + (dir ? (n - 1 - (q0 + q)) : (q0 + q))] = conv<TV>(hi);
+            }
         }
     }
     bool ok = true;
@@ -737,7 +800,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
 template <int KD, bool STAGE>
 static cudaError_t solve_mixed_launch(const InvTab& tab, int nrows, const void* in, int in_prec, void* out,
                                       int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
-                                      int check_broken, cudaStream_t s, float4* v0s) {
+                                      int check_broken, cudaStream_t s, float4* v0s, const void* bpart, int bG) {
     if (out_prec != 1) return cudaErrorInvalidValue;
     size_t smem = 0;
     for (int c = 0; c < tab.nchunks; ++c)
@@ -751,7 +814,7 @@ static cudaError_t solve_mixed_launch(const InvTab& tab, int nrows, const void* 
             if (ea != cudaSuccess) return ea;                                                                    \
         }                                                                                                        \
         cudaError_t el = launch_pdl(kern, grid, block, smem, s, tab, (const TI_*)in, (float2*)out, (TV_*)vstore,  \
-                                    ctrl, dir, scale_mode, check_broken, v0s);                                   \
+                                    ctrl, dir, scale_mode, check_broken, v0s, (const float4*)bpart, bG);         \
         return el != cudaSuccess ? el : cudaGetLastError();                                                      \
     }
     // in: the FP64 first vector (with its FP64 copy stored) or a complex64 vector
@@ -765,7 +828,7 @@ static cudaError_t solve_mixed_launch(const InvTab& tab, int nrows, const void* 
 template <int KD, bool R64, bool STAGE>
 static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in, int in_prec, void* out,
                                     int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir,
-                                    int scale_mode, int check_broken, cudaStream_t s) {
+                                    int scale_mode, int check_broken, cudaStream_t s, const void* bpart, int bG) {
     const int P = R64 ? tab.refine : 0;
     size_t smem = 0;
     for (int c = 0; c < tab.nchunks; ++c)
@@ -779,7 +842,7 @@ static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in
             if (ea != cudaSuccess) return ea;                                                                    \
         }                                                                                                        \
         cudaError_t el = launch_pdl(kern, grid, block, smem, s, tab, (const TI_*)in, (TO_*)out, (TV_*)vstore,     \
-                                    ctrl, dir, scale_mode, check_broken);                                        \
+                                    ctrl, dir, scale_mode, check_broken, (const double*)bpart, bG);              \
         return el != cudaSuccess ? el : cudaGetLastError();                                                      \
     }
     // combinations the runtime uses: refined solves store double2 (or nothing)
@@ -797,30 +860,30 @@ static cudaError_t solve_inv_launch(const InvTab& tab, int nrows, const void* in
 template <int KD>
 static cudaError_t solve_inv_kd(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
                                 int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
-                                int check_broken, cudaStream_t s, float4* v0s) {
+                                int check_broken, cudaStream_t s, float4* v0s, const void* bpart, int bG) {
     if (refine64) {
         if (tab.stage)
             return solve_inv_launch<KD, true, true>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
-                                                    scale_mode, check_broken, s);
+                                                    scale_mode, check_broken, s, bpart, bG);
         return solve_inv_launch<KD, true, false>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
-                                                 scale_mode, check_broken, s);
+                                                 scale_mode, check_broken, s, bpart, bG);
     }
     if (tab.stage)
         return solve_mixed_launch<KD, true>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
-                                            scale_mode, check_broken, s, v0s);
+                                            scale_mode, check_broken, s, v0s, bpart, bG);
     return solve_mixed_launch<KD, false>(tab, nrows, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,
-                                         scale_mode, check_broken, s, v0s);
+                                         scale_mode, check_broken, s, v0s, bpart, bG);
 }
 
 cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const void* in, int in_prec, void* out,
                              int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
-                             int check_broken, cudaStream_t s, float4* v0s) {
+                             int check_broken, cudaStream_t s, float4* v0s, const void* bpart, int bG) {
     count_launch();
     switch (tab.kd) {
 #define GB_KD(K)                                                                                                 \
     case K:                                                                                                      \
         return solve_inv_kd<K>(tab, nrows, refine64, in, in_prec, out, out_prec, vstore, v_prec, ctrl, dir,      \
-                               scale_mode, check_broken, s, v0s);
+                               scale_mode, check_broken, s, v0s, bpart, bG);
         GB_KD(1) GB_KD(2) GB_KD(3) GB_KD(4) GB_KD(5) GB_KD(6) GB_KD(7) GB_KD(8)
 #undef GB_KD
         default: return cudaErrorInvalidValue;
