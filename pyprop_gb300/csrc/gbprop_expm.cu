@@ -348,7 +348,20 @@ static cudaError_t launch_df(Ctrl* ctrl, double* H, int m, const SchedEntry* sch
 cudaError_t launch_expm_df(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int cluster, cudaStream_t s) {
     if (cluster == 16) return launch_df<16>(ctrl, H, m, sched, s);
     if (cluster == 8) return launch_df<8>(ctrl, H, m, sched, s);
+    if (cluster == 1) return launch_df<1>(ctrl, H, m, sched, s);   // one CTA (batches)
     return cudaErrorInvalidValue;
+}
+
+bool expm_df_single_fits(int m) {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k_expm_cluster_df<1>) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (size_t)7 * m * m * sizeof(float4) + fa.sharedSizeBytes + 1024 <= (size_t)optin;
 }
 
 }  // namespace gbprop

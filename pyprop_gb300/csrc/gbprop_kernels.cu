@@ -1441,6 +1441,11 @@ cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, i
     count_launch();
     const int cl = max_cluster >= 8 ? expm_cluster_size(m) : 0;
     if (df32 && (cl == 16 || cl == 8) && cl <= max_cluster) return launch_expm_df(ctrl, H, m, sched, cl, s);
+    if (df32 && cl == 0) {
+        static int fits[kMaxBasis + 1];              // 0 unknown, 1 yes, 2 no
+        if (m >= 1 && m <= kMaxBasis && fits[m] == 0) fits[m] = expm_df_single_fits(m) ? 1 : 2;
+        if (m >= 1 && m <= kMaxBasis && fits[m] == 1) return launch_expm_df(ctrl, H, m, sched, 1, s);
+    }
     if (cl == 16 && max_cluster >= 16) return launch_expm_cl<16>(ctrl, H, m, sched, s);
     if (cl == 8) return launch_expm_cl<8>(ctrl, H, m, sched, s);
     const size_t smem = (size_t)5 * m * m * sizeof(double2);
