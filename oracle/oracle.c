@@ -379,6 +379,8 @@ int orc_pade_exponential(int m, const cplx* A, int order, cplx* out) {
  * s = max(0, ceil(log2(max |A_ij|))), A /= 2^s, Pade, then s squarings.
  * Returns the LU info; *scaling_out receives s. */
 int orc_scaling_pade_exponential(int m, const cplx* Ain, int order, cplx* out, int* scaling_out) {
+    if (scaling_out) *scaling_out = 0;
+    if (m <= 0) return 0;
     long mm = (long)m * m;
     cplx* A = (cplx*)malloc(mm * sizeof(cplx));
     cplx* T = (cplx*)malloc(mm * sizeof(cplx));
