@@ -244,8 +244,36 @@ def cpu_baseline_sample(workload, budget_s=12.0):
         psi, _ = op.advance(psi, m, dt, [0.0])
         n += 1
     el = time.perf_counter() - t0
+    # the same restatement on one thread (a few steps of the workload, bounded)
+    orc.set_threads(1)
+    n1, t1 = 0, time.perf_counter()
+    while time.perf_counter() - t1 < budget_s / 3 and n1 < 200:
+        psi, _ = op.advance(psi, m, dt, [0.0])
+        n1 += 1
+    el1 = time.perf_counter() - t1
+    orc.set_threads(threads)
     return {"value": n / el, "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": "%d Krylov steps of the workload in %.1f s (oracle/oracle.c, OpenMP)" % (n, el)}
+            "sample": "%d Krylov steps of the workload in %.1f s (oracle/oracle.c, OpenMP)" % (n, el),
+            "single_thread": {"value": n1 / el1, "unit": "steps/s", "cores": 1,
+                              "sample": "%d Krylov steps in %.1f s" % (n1, el1)},
+            "host": host_cpu()}
+
+
+def host_cpu():
+    """The host's CPU model and core count (as the OS reports them)."""
+    import platform
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":", 1)[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return {"model": model or platform.processor() or platform.machine(), "machine": platform.machine(),
+            "nproc": os.cpu_count()}
 
 
 def run_batch(args, rank, world, local):
