@@ -586,22 +586,23 @@ def measure_single(args, precision, device, world, with_e2e=True):
     B_mv, B_step = algorithmic_bytes(N, m, elem, band_coef + solve_coef)
     src = psi0.clone()
     dst = torch.empty_like(src)
-    reps = 100                                   # each launch timed on its own; median reported
+    # average launch duration over 100 back-to-back launches, CUDA events on the launching stream
+    # (events around each launch would add their own gaps to a ~20 us kernel)
+    reps = 100
     for balanced in (0, 1):
         for _ in range(5):
             h.matvec(src, dst, 0.1, balanced=bool(balanced))
         torch.cuda.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
-        for e0, e1 in ev:
-            e0.record(stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
             h.matvec(src, dst, 0.1, balanced=bool(balanced))
-            e1.record(stream)
+        e1.record(stream)
         torch.cuda.synchronize()
-        t_med = float(np.median([e0.elapsed_time(e1) for e0, e1 in ev]))
         if balanced:
-            t_bal = t_med
+            t_bal = e0.elapsed_time(e1) / reps
         else:
-            t_band = t_med
+            t_band = e0.elapsed_time(e1) / reps
     peak, peak_kind = load_peaks()
     band_bytes = 2 * N * elem + band_coef
     achieved = band_bytes / (t_band * 1e-3) / 1e9
