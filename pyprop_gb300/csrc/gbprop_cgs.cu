@@ -225,13 +225,13 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
 }
 
 // ---------------------------------------------------------------------------
-// Complex64 basis (FP32-mixed path).  The same three phases, with every inner product,
-// partial sum and norm formed by error-free FP32 transformations (hi + lo pairs): on this
+// Complex64 basis (FP32-mixed path).  The same phases, with every inner product, partial
+// sum and norm share formed by error-free FP32 transformations (hi + lo pairs): on this
 // GPU the FP64 pipe retires two thread operations per clock per SM, so FP64 adds in
 // reductions (every lane of every warp) cost as much as the products themselves.  The
 // first vector comes split into FP32 pairs (v0s, float4 re_hi, im_hi, re_lo, im_lo);
 // partials are float4 (re_hi, re_lo, im_hi, im_lo) per (vector, CTA).  Only single
-// threads touch FP64 (the Hessenberg entries, beta).
+// threads touch FP64 (the Hessenberg entries).
 constexpr int kCgsWarps = kFuseThreads / 32;
 constexpr int kCgsItems = 64;
 
