@@ -6,8 +6,12 @@
 //     gbprop_solve.cu;
 //   * the tensor-potential matvec applies real band slots to complex vectors
 //     (2 FMA per band entry instead of 4) with the source halo tile in smem;
-//   * Gram-Schmidt reductions are two-level (block partials + last-block
-//     finalize in fixed order: deterministic, no atomics on values).
+//   * Gram-Schmidt runs as one cooperative kernel per Arnoldi step
+//     (gbprop_cgs.cu); the dot / update / finalize kernels here serve
+//     re-orthogonalisation and batches, with two-level reductions (block
+//     partials + last-block finalize in fixed order: deterministic, no atomics
+//     on values);
+//   * the FP32-mixed path's exponential is in double-float (gbprop_expm.cu).
 #include "gbprop_internal.h"
 #include "gbprop_device.cuh"
 
