@@ -470,7 +470,8 @@ def run_adjoint(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 200 for a single problem, 20 for the 256-problem batch)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbprop", choices=["gbprop", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32-mixed"])
@@ -481,6 +482,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed arm of the default run")
     ap.add_argument("--no-precision-report", action="store_true")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 20 if args.workload == "batch" else 200
     args.warmup = max(args.warmup, 3)
 
     rank, world, local = _dist()
