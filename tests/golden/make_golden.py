@@ -14,7 +14,17 @@ arrays those methods fill (plus ScaleAndTranslate, core/transform/bspline/bsplin
 supplied with matplotlib's published semantics (closed interval, npts =
 round((xfin - xini)/delta) + 1).
 
-Writes tests/golden/setup_golden.npz.  Usage: python tests/golden/make_golden.py
+Writes tests/golden/setup_golden.npz.
+
+It also runs the reference's storage and pair generators (pure Python):
+  pyprop/tensorpotential/GeometryInfo.py        GeometryInfoCommonBandedNonHermitian.GetBasisPairs
+  pyprop/tensorpotential/basis/ReducedSphericalHarmonic.py
+                                                GeometryInfoReducedSphHarmSelectionRule.GetBasisPairs
+with a stand-in for the compiled ReducedSphericalTools exposing GetSize() = LMax - |M|
+(core/transform/reducedspherical/reducedsphericaltools.h:53), and writes
+tests/golden/geometry_golden.npz.
+
+Usage: python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -143,7 +153,42 @@ def main():
     print("wrote", OUT, len(out), "arrays")
 
 
+GEO_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "geometry_golden.npz")
+BANDNH_CASES = ((9, 2), (20, 6), (103, 6), (5, 6), (1, 0))
+SELECTION_CASES = ((3, 0), (9, 0), (63, 0), (5, 2), (1, 0))
+
+
+def geometry():
+    ns = {"__name__": "pyprop_ref_geometry", "xrange": range}
+    exec("from numpy import *", ns)
+    for rel in (("tensorpotential", "GeometryInfo.py"), ("tensorpotential", "basis", "ReducedSphericalHarmonic.py")):
+        path = os.path.join(REF, "pyprop", *rel)
+        with open(path) as f:
+            exec(compile(_py2_to_py3(f.read()), path, "exec"), ns)
+
+    class _Tools:
+        """Stand-in for core.ReducedSphericalTools: only GetSize() is used by the pair generator."""
+
+        def __init__(self, lmax, m):
+            self.lmax, self.m = lmax, m
+
+        def GetSize(self):
+            return self.lmax - abs(self.m)
+
+    out = {}
+    for n, k in BANDNH_CASES:
+        g = ns["GeometryInfoCommonBandedNonHermitian"](n, k, False)
+        out["bandnh_pairs_%d_%d" % (n, k)] = np.asarray(g.GetBasisPairs())
+    for lmax, m in SELECTION_CASES:
+        g = ns["GeometryInfoReducedSphHarmSelectionRule"](_Tools(lmax, m), False)
+        out["selection_pairs_%d_%d" % (lmax, m)] = np.asarray(g.GetBasisPairs())
+        out["selection_count_%d_%d" % (lmax, m)] = np.array(g.GetGlobalBasisPairCount())
+    np.savez_compressed(GEO_OUT, **out)
+    print("wrote", GEO_OUT, len(out), "arrays")
+
+
 if __name__ == "__main__":
     if not os.path.isdir(REF):
         sys.exit("reference tree not present; the committed fixture is used as is")
     main()
+    geometry()

@@ -135,3 +135,24 @@ def test_laser_function_values():
     t = 0.3 * T
     want = sec.amplitude * np.sin(np.pi * t / T) ** 2 * -np.cos(sec.frequency * t)
     assert abs(pp.LaserFunctionVelocity(sec, t) - want) < 1e-15
+
+
+GEO = np.load(os.path.join(os.path.dirname(__file__), "golden", "geometry_golden.npz"))
+
+
+@pytest.mark.parametrize("n,k", [(9, 2), (20, 6), (103, 6), (5, 6), (1, 0)])
+def test_bandnh_pairs_golden(n, k):
+    """BandNH storage order against the reference's own GeometryInfoCommonBandedNonHermitian
+    (GeometryInfo.py:433-454), run by tests/golden/make_golden.py."""
+    from pyprop_gb300.tensorpotential import bandnh_pairs
+    np.testing.assert_array_equal(bandnh_pairs(n, k), GEO["bandnh_pairs_%d_%d" % (n, k)])
+
+
+@pytest.mark.parametrize("lmax,m", [(3, 0), (9, 0), (63, 0), (5, 2), (1, 0)])
+def test_dipole_selection_pairs_golden(lmax, m):
+    """Dipole selection-rule pairs against the reference's own
+    GeometryInfoReducedSphHarmSelectionRule (basis/ReducedSphericalHarmonic.py:5-45)."""
+    from pyprop_gb300.basis.sphharm import ReducedSphericalTools, selection_rule_pairs
+    got = selection_rule_pairs(ReducedSphericalTools(lmax, m))
+    np.testing.assert_array_equal(got, GEO["selection_pairs_%d_%d" % (lmax, m)])
+    assert len(got) == int(GEO["selection_count_%d_%d" % (lmax, m)])
