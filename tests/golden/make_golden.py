@@ -22,7 +22,8 @@ It also runs the reference's storage and pair generators (pure Python):
                                                 GeometryInfoReducedSphHarmSelectionRule.GetBasisPairs
 with a stand-in for the compiled ReducedSphericalTools exposing GetSize() = LMax - |M|
 (core/transform/reducedspherical/reducedsphericaltools.h:53), and writes
-tests/golden/geometry_golden.npz.
+tests/golden/geometry_golden.npz; and the velocity-gauge pulse LaserFunctionVelocity of the
+helium_stabilization_sae example -> tests/golden/laser_golden.npz.
 
 Usage: python tests/golden/make_golden.py
 """
@@ -187,8 +188,36 @@ def geometry():
     print("wrote", GEO_OUT, len(out), "arrays")
 
 
+LASER_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "laser_golden.npz")
+
+
+def laser():
+    """LaserFunctionVelocity of examples/tensor/helium_stabilization_sae/example.py:220-230, its
+    source text cut out of the script (the rest is Python 2 and needs the compiled core), on a
+    time grid that includes the pulse edges, with and without the optional phase key."""
+    path = os.path.join(REF, "examples", "tensor", "helium_stabilization_sae", "example.py")
+    src = open(path).read()
+    m = re.search(r"^def LaserFunctionVelocity\(.*?(?=^\S)", src, flags=re.M | re.S)
+    ns = {}
+    exec("from numpy import *", ns)
+    exec(compile(m.group(0), path, "exec"), ns)
+    out = {}
+    for name, kw in (("nophase", dict(amplitude=0.877, frequency=0.057, pulse_duration=8 * 2 * np.pi / 0.057)),
+                     ("phase", dict(amplitude=1.754, frequency=0.057, pulse_duration=20 * 2 * np.pi / 0.057,
+                                    phase=0.3))):
+        T = kw["pulse_duration"]
+        t = np.concatenate([[-1.0, 0.0, T * (1 - 1e-12), T, T + 1.0], np.linspace(0.0, T, 97)])
+        out["laser_%s_t" % name] = t
+        out["laser_%s_f" % name] = np.array([ns["LaserFunctionVelocity"](_Conf(**kw), x) for x in t])
+        for k, v in kw.items():
+            out["laser_%s_cfg_%s" % (name, k)] = np.array(v)
+    np.savez_compressed(LASER_OUT, **out)
+    print("wrote", LASER_OUT, len(out), "arrays")
+
+
 if __name__ == "__main__":
     if not os.path.isdir(REF):
         sys.exit("reference tree not present; the committed fixture is used as is")
     main()
     geometry()
+    laser()

@@ -156,3 +156,21 @@ def test_dipole_selection_pairs_golden(lmax, m):
     got = selection_rule_pairs(ReducedSphericalTools(lmax, m))
     np.testing.assert_array_equal(got, GEO["selection_pairs_%d_%d" % (lmax, m)])
     assert len(got) == int(GEO["selection_count_%d_%d" % (lmax, m)])
+
+
+LASER = np.load(os.path.join(os.path.dirname(__file__), "golden", "laser_golden.npz"))
+
+
+@pytest.mark.parametrize("case", ["nophase", "phase"])
+def test_laser_function_golden(case):
+    """The velocity-gauge pulse against the reference's own LaserFunctionVelocity
+    (examples/tensor/helium_stabilization_sae/example.py:220-230), including both pulse edges."""
+    class Sec:
+        pass
+    sec = Sec()
+    prefix = "laser_%s_cfg_" % case
+    for k in LASER.files:
+        if k.startswith(prefix):
+            setattr(sec, k[len(prefix):], float(LASER[k]))
+    got = np.array([pp.LaserFunctionVelocity(sec, t) for t in LASER["laser_%s_t" % case]])
+    np.testing.assert_allclose(got, LASER["laser_%s_f" % case], rtol=1e-14, atol=1e-17)
