@@ -186,9 +186,54 @@ def build_problem(workload, precision, device):
     return prob
 
 
+def run_reference_batch(args):
+    """The batch workload on the CPU restatement: the same seeded problems, each advanced by the
+    oracle on all host threads; a bounded sample of problems and steps is timed and extrapolated
+    to the whole batch (batch steps/s = 1 / sum over problems of the per-problem step time)."""
+    from oracle import oracle as orc
+    from pyprop_gb300.batch import random_batch
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    probs = random_batch(args.batch_size, seed=20261204)
+    sample = probs[:min(len(probs), 8)]
+    per = []
+    for p in sample:
+        pots = [dict(kind=orc.ORC_DIAG_BANDNH, data=p.static, pairs=None, timedep=False),
+                dict(kind=orc.ORC_SIMP_BANDNH, data=p.dipole, pairs=p.pairs, timedep=True)]
+        op = orc.Operator(p.nl, p.nr, p.kd, p.kb, p.cholesky_band().astype(np.complex128), pots)
+        psi = p.initial_state()
+        for _ in range(min(args.warmup, 1)):
+            psi, _ = op.advance(psi, p.m, p.dt, [0.1])
+        n = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(n):
+            psi, _ = op.advance(psi, p.m, p.dt, [0.1])
+        per.append((time.perf_counter() - t0) / n)
+    step_s = float(np.mean(per)) * len(probs)
+    v = 1.0 / step_s
+    line = {
+        "impl": "reference", "metric": METRIC + ", batch", "value": v, "unit": "batch steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": "hydrogen_velocity_batch", "problems": len(probs), "precision": "fp64"},
+        "cpu_baseline": {"value": v, "unit": "batch steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d of %d problems, %d steps each, extrapolated to the batch (oracle/oracle.c, "
+                                   "OpenMP)" % (len(sample), len(probs), max(1, min(args.steps, 3)))},
+        "e2e": {"value": v, "unit": "batch steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     """CPU restatement of the reference step (oracle/), all host threads."""
     if rank != 0:
+        return
+    if args.workload == "batch":
+        run_reference_batch(args)
+        return
+    if args.workload == "adjoint":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference computes no gradients (no adjoint "
+                                                             "or derivative of the propagation)"}), flush=True)
         return
     import pyprop_gb300 as pp
     from oracle import oracle as orc

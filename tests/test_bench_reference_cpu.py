@@ -26,3 +26,19 @@ def test_reference_arm_json_line():
     assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["value"] == d["value"]
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["config"]["workload"] == "hydrogen_velocity_small"
+
+
+def test_reference_arm_batch_and_adjoint():
+    """The batch workload's reference arm times the restatement on a sample of the same seeded
+    problems (batch steps/s); the adjoint has no reference counterpart and says so."""
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "batch", "--batch-size", "12",
+                        "--steps", "2", "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    assert d["impl"] == "reference" and d["unit"] == "batch steps/s" and d["value"] > 0
+    assert d["config"]["problems"] == 12 and d["e2e"]["h2d_bytes_per_step"] == 0
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "adjoint"], cwd=ROOT,
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0
+    d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    assert d["impl"] == "reference" and "unavailable" in d
