@@ -110,7 +110,15 @@ gbprop_status gbprop_finalize(gbprop_handle h);
  *   psi <- U^-1 pAMP_m(U psi, dt; H(t_n))   for n = 0..nsteps-1
  * scalings[n] (HOST array) is the time function at the start of step n
  * (TensorPotential.py:98-100 with t = PropagatedTime).  dt may be complex
- * (imaginary time).  Asynchronous on the handle's stream. */
+ * (imaginary time).  Asynchronous on the handle's stream.
+ *
+ * Failures on the device (the reference throws at once, pamp.h:544-550) are
+ * returned as GBPROP_ELU (singular Pade denominator), GBPROP_ENONFINITE (NaN/Inf
+ * norm or Hessenberg entry) or GBPROP_ETIMEOUT (a bounded device-side wait gave
+ * up) by the first call on the handle after the GPU has finished the failing
+ * step: a later gbprop_advance (without waiting), or at the latest
+ * gbprop_synchronize, gbprop_advance_host or gbprop_get_stats (which wait).  A
+ * reported failure is cleared, so the handle stays usable. */
 gbprop_status gbprop_advance(gbprop_handle h, void* psi, int nsteps, const double* scalings,
                              double dt_re, double dt_im);
 
@@ -135,7 +143,48 @@ gbprop_status gbprop_reset_stats(gbprop_handle h);
 /* Copy the last step's (scaled, -i*dt*H) Hessenberg matrix, m*m complex128
  * row-major, to HOST memory (pAMP::GetHessenbergMatrix, pamp.h:197-200). */
 gbprop_status gbprop_get_hessenberg(gbprop_handle h, double* out);
+/* Waits for the handle's work; returns a device-side failure of it (see gbprop_advance). */
 gbprop_status gbprop_synchronize(gbprop_handle h);
+
+/* Per-phase times of one propagation step: the pAMP timers ("Operator", "InnerProduct",
+ * "PadeExponential", pamp.h:149-151, printed by PrintStatistics, :671-687), split by kernel
+ * phase.  gbprop_time_step runs one step (psi <- U^-1 pAMP(U psi)) on a DEVICE wavefunction
+ * outside the step's CUDA graph, with an event after every launch, waits for it and fills
+ * `out`: ms[p] and count[p] are the time and the launches of phase p (the time between the
+ * event before a launch and the one after it), total_ms their sum, launches all kernel
+ * launches.  Slower than gbprop_advance (no graph); the same arithmetic. */
+typedef enum {
+    GBPROP_PHASE_SOLVE = 0,         /* overlap-factor solves (U^-1, U^-T; state transform) */
+    GBPROP_PHASE_BAND = 1,          /* TensorPotential band matvec */
+    GBPROP_PHASE_GRAM_SCHMIDT = 2,  /* inner products, update, norms, Hessenberg column */
+    GBPROP_PHASE_EXPONENTIAL = 3,   /* Pade scaling-and-squaring of the Hessenberg matrix */
+    GBPROP_PHASE_COMBINE = 4,       /* psi = beta0 V exp(-i dt H) e1 */
+    GBPROP_PHASE_OTHER = 5,         /* U psi, step bookkeeping */
+    GBPROP_PHASE_COUNT = 6
+} gbprop_phase;
+typedef struct {
+    double ms[GBPROP_PHASE_COUNT];
+    int count[GBPROP_PHASE_COUNT];
+    double total_ms;
+    long long launches;
+} gbprop_step_timers;
+gbprop_status gbprop_time_step(gbprop_handle h, void* psi, double scaling, double dt_re, double dt_im,
+                               gbprop_step_timers* out);
+
+/* Test hooks for the failure paths, no counterpart in the reference (its failures are
+ * CPU exceptions).  Neither faults nor hangs the GPU; both stay set until changed.
+ *   GBPROP_DEBUG_WAIT_LIMIT  value = polls of the first bounded wait of each launch (the
+ *                            bulk-copy staging wait, the cooperative grid barrier); 0 restores
+ *                            the default, a negative value makes those waits give up at once
+ *                            (the launch records the timeout and returns: GBPROP_ETIMEOUT)
+ *   GBPROP_DEBUG_INJECT_LU   value != 0: every Pade solve reports a zero pivot, as zgetrf's
+ *                            info != 0 in pamp.h:544-550 (GBPROP_ELU); 0 clears it
+ * Synchronises the handle's stream. */
+typedef enum {
+    GBPROP_DEBUG_WAIT_LIMIT = 0,
+    GBPROP_DEBUG_INJECT_LU = 1
+} gbprop_debug_key;
+gbprop_status gbprop_debug_set(gbprop_handle h, int key, long long value);
 
 /* Statistics of one gbprop_expokit_advance call (Expokit's zgexpv diagnostics). */
 typedef struct {
@@ -180,6 +229,9 @@ gbprop_status gbprop_batch_create(gbprop_batch* out, const gbprop_handle* proble
  * dt: count x 2 HOST array (re, im of each problem's time step). */
 gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps, const double* scalings,
                                    const double* dt);
+/* Waits for the batch's work; returns a device-side failure of any member (see
+ * gbprop_advance; gbprop_batch_advance also returns one once it is known, without waiting). */
+gbprop_status gbprop_batch_synchronize(gbprop_batch b);
 gbprop_status gbprop_batch_destroy(gbprop_batch b);
 
 /* Stateless kernel ABI: TensorPotentialMultiply_<S0>_BandNH
@@ -205,9 +257,9 @@ gbprop_status gbprop_block_inner_product(int precision, const void* V, long n, i
                                          double* out, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Allocation-free variant of gbprop_block_inner_product, for callers that cannot
- * allocate device memory when they need it: code running while a CUDA graph is
- * captured (cudaMalloc cannot be captured), memory pools or custom allocators that
- * call back into this library, hosts that hand over only fixed buffers.  No
+ * allocate device memory when they need it: memory pools or custom allocators that
+ * call back into this library (allocating there would re-enter the allocator), and
+ * hosts that hand over only fixed buffers and allow no allocation after start-up.  No
  * counterpart in the reference (its temp vector is always caller-allocated).
  * Same arguments and results as gbprop_block_inner_product minus the workspace:
  * the reduction scratch is one fixed array of 1024 doubles + a counter word in

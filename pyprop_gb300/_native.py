@@ -21,6 +21,8 @@ FP32_MIXED = 1
 STORAGE_DIAG = 0
 STORAGE_IDENT = 1
 STORAGE_SIMP = 2
+DEBUG_WAIT_LIMIT = 0
+DEBUG_INJECT_LU = 1
 
 
 class GbpropError(RuntimeError):
@@ -53,6 +55,18 @@ class ExpokitStats(C.Structure):
     ]
 
 
+PHASES = ["solve", "band", "gram_schmidt", "exponential", "combine", "other"]
+
+
+class StepTimers(C.Structure):
+    _fields_ = [
+        ("ms", C.c_double * 6),
+        ("count", C.c_int * 6),
+        ("total_ms", C.c_double),
+        ("launches", C.c_longlong),
+    ]
+
+
 _lib = None
 
 # name -> (restype, argtypes)
@@ -74,6 +88,9 @@ _PROTOS = {
     "gbprop_reset_stats": (C.c_int, [C.c_void_p]),
     "gbprop_get_hessenberg": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gbprop_synchronize": (C.c_int, [C.c_void_p]),
+    "gbprop_debug_set": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong]),
+    "gbprop_time_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                   C.POINTER(StepTimers)]),
     "gbprop_tensor_multiply_bandnh": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double,
                                                 C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "gbprop_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
@@ -82,6 +99,7 @@ _PROTOS = {
     "gbprop_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_void_p]),
     "gbprop_batch_advance": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.c_void_p]),
     "gbprop_batch_destroy": (C.c_int, [C.c_void_p]),
+    "gbprop_batch_synchronize": (C.c_int, [C.c_void_p]),
     "gbprop_block_inner_product_workspace": (C.c_size_t, [C.c_long, C.c_int]),
     "gbprop_block_inner_product": (C.c_int, [C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
@@ -211,7 +229,23 @@ class Handle:
         return out
 
     def synchronize(self):
+        """Wait for the handle's work; raises GbpropError for a device-side failure of it."""
         check(lib().gbprop_synchronize(self._h))
+
+    def time_step(self, psi_dev, scaling, dt):
+        """One step outside the graph with an event per launch; returns
+        {phase: (ms, launches)}, plus 'total_ms' and 'launches'."""
+        dt = complex(dt)
+        t = StepTimers()
+        check(lib().gbprop_time_step(self._h, ptr(psi_dev), float(scaling), dt.real, dt.imag, C.byref(t)))
+        out = {name: (t.ms[k], t.count[k]) for k, name in enumerate(PHASES)}
+        out["total_ms"] = t.total_ms
+        out["launches"] = t.launches
+        return out
+
+    def debug_set(self, key, value):
+        """Test hooks of the failure paths (DEBUG_WAIT_LIMIT, DEBUG_INJECT_LU; see gbprop.h)."""
+        check(lib().gbprop_debug_set(self._h, int(key), int(value)))
 
     def expokit_advance(self, psi_dev, scalings, dt, tol, anorm):
         """Expokit steps (Krylov dimension = this handle's basis size - 1); returns ExpokitStats."""
@@ -258,6 +292,10 @@ class Batch:
         d = np.ascontiguousarray(np.array([[complex(x).real, complex(x).imag] for x in dts], dtype=np.float64))
         arr = (C.c_void_p * P)(*[p.data_ptr() for p in psis])
         check(lib().gbprop_batch_advance(self._b, arr, int(s.shape[1]), ptr(s), ptr(d)))
+
+    def synchronize(self):
+        """Wait for the batch; raises GbpropError for a device-side failure of any member."""
+        check(lib().gbprop_batch_synchronize(self._b))
 
 
 def launch_count():

@@ -170,6 +170,10 @@ class BatchPropagator:
             self.time[p] = t
         self.batch.advance(self.psi, scal, [p.dt for p in self.problems])
 
+    def synchronize(self):
+        """Wait for the batch; raises GbpropError for a device-side failure of any problem."""
+        self.batch.synchronize()
+
     def scalings(self, p, nsteps, t0=0.0):
         prob = self.problems[p]
         out, t = [], t0

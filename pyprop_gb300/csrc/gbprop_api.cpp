@@ -16,6 +16,7 @@
 #include <cfloat>
 #include <cmath>
 #include <complex>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -106,6 +107,16 @@ struct gbprop_ctx {
     unsigned* d_gridbar = nullptr;    // its grid-barrier words
     std::vector<void*> allocs;
 
+    // per-phase timing of one un-captured step (gbprop_time_step): when `timing` is set, every
+    // launch of the step sequence is followed by an event, tagged with its phase
+    std::vector<std::pair<int, cudaEvent_t>>* timing = nullptr;
+    std::vector<cudaEvent_t> tick_pool;
+    // device error flags (Ctrl::lu_info, nonfinite, wait_timeout) copied to pinned host memory
+    // after every advance; read once the copy's event has completed (see device_errors)
+    int* h_flags = nullptr;
+    cudaEvent_t ev_flags = nullptr;
+    bool flags_armed = false;
+
     cudaGraphExec_t graph = nullptr;      // one step on x (independent of the caller's buffers)
     cudaGraphExec_t graph_arnoldi = nullptr;   // Expokit: the Arnoldi part alone (m+1 vectors)
     long long arnoldi_launches = 0;
@@ -121,6 +132,9 @@ struct gbprop_ctx {
         for (void* p : allocs) cudaFree(p);
         if (ev_in) cudaEventDestroy(ev_in);
         if (ev_out) cudaEventDestroy(ev_out);
+        if (ev_flags) cudaEventDestroy(ev_flags);
+        if (h_flags) cudaFreeHost(h_flags);
+        for (cudaEvent_t e : tick_pool) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
     // order the handle's work after / before the caller's stream
@@ -491,6 +505,16 @@ gbprop_status check_handle(gbprop_handle h, bool need_final) {
         if (_e != cudaSuccess) return fail(GBPROP_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
     } while (0)
 
+// Phase tag of a launch for gbprop_time_step (the pAMP timers "Operator", "InnerProduct",
+// "PadeExponential" of pamp.h:149-151, split finer).
+void tick(gbprop_ctx* h, int phase) {
+    if (!h->timing) return;
+    const size_t k = h->timing->size();
+    if (k + 1 >= h->tick_pool.size()) return;          // the last event marks the start
+    cudaEventRecord(h->tick_pool[k], h->stream);
+    h->timing->push_back({phase, h->tick_pool[k]});
+}
+
 // Chunking of the inverse solve.  `wide` spreads one problem's rows over the GPU: the
 // chunk count minimises (waves of CTAs) x (FP64 residual elements of one CTA, halo
 // included), the refinement being FP64-issue-bound; otherwise (batches, where other
@@ -583,6 +607,7 @@ const void* kop(gbprop_ctx* h) {
 // per-step rounding of the state.
 gbprop_status enqueue_enter(gbprop_ctx* h, void* psi, cudaStream_t s) {
     GB_LAUNCH(launch_tbmv(0, h->kd, h->d_ud_phys, h->nl, h->nr, psi, h->kprec(), h->d_x, 0, s));
+    tick(h, GBPROP_PHASE_OTHER);
     return GBPROP_OK;
 }
 
@@ -592,6 +617,7 @@ gbprop_status enqueue_leave(gbprop_ctx* h, void* psi, cudaStream_t s) {
     cudaError_t e = ssolve(h, 0, h->d_x, 0, psi, h->kprec());
     h->stream = keep;
     if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("ssolve: ") + cudaGetErrorString(e));
+    tick(h, GBPROP_PHASE_SOLVE);
     return GBPROP_OK;
 }
 
@@ -606,12 +632,14 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
     char* V = (char*)h->d_V;
     const size_t vbytes = (size_t)N * h->kelem();
     GB_LAUNCH(launch_step_begin(h->d_ctrl, h->d_H, m, s));
+    tick(h, GBPROP_PHASE_OTHER);
     // the fused form hands beta to the next solve and (complex64) reads the split first vector:
     // both only the inverse-band solve provides
     const bool fused = h->cgs_grid > 0 && !dorth && h->expm_max_cluster > 1 && h->inv_ok;
     if (fused) GB_CUDA(cudaMemsetAsync(h->d_gridbar, 0, 2 * sizeof(unsigned), s));
     // beta0 = ||x||
     GB_LAUNCH(launch_norm(0, h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
+    tick(h, GBPROP_PHASE_GRAM_SCHMIDT);
     for (int J = 0; J < m; ++J) {
         const void* in = J == 0 ? (const void*)h->d_x : (const void*)h->d_r;
         const int in_prec = J == 0 ? 0 : kp;
@@ -625,14 +653,18 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
             GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, h->d_v0, 0, 1, 1, fused ? h->d_v0s : nullptr));
         else
             GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1, nullptr, bpart));
+        tick(h, GBPROP_PHASE_SOLVE);
         // y = sum_t c_t s_t A_t s
         GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, h->d_sched, h->d_ctrl, 0.0, 1, s));
+        tick(h, GBPROP_PHASE_BAND);
         // w = U^-T y
         GB_LAUNCH(ksolve(h, 1, h->d_y, kp, h->d_r, kp, nullptr, kp, 0, 1));
+        tick(h, GBPROP_PHASE_SOLVE);
         // classical Gram-Schmidt against v_0..v_J
         if (fused) {
             GB_LAUNCH(launch_arnoldi_cgs(kp, V, h->d_v0s, N, J, m, h->d_r, h->d_cgs_part, h->d_gridbar, h->d_ctrl,
                                          h->d_H, J < m - 1, h->cgs_grid, h->cgs_cache, s));
+            tick(h, GBPROP_PHASE_GRAM_SCHMIDT);
             continue;
         }
         GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0,
@@ -649,6 +681,7 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
             }
         }
         GB_LAUNCH(launch_arnoldi_finalize(h->d_ctrl, h->d_H, m, J, dorth, brk_tol, s));
+        tick(h, GBPROP_PHASE_GRAM_SCHMIDT);
     }
     return GBPROP_OK;
 }
@@ -662,9 +695,12 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
     char* V = (char*)h->d_V;
     if (gbprop_status st = enqueue_arnoldi(h, h->double_orth, std::sqrt(DBL_EPSILON))) return st;   // pamp.h:79
     GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s, h->prec != GBPROP_FP64));
+    tick(h, GBPROP_PHASE_EXPONENTIAL);
     // x <- beta0 V exp(-i dt H) e1
     GB_LAUNCH(launch_combine(kp, V, h->d_v0, N, h->d_ctrl, h->d_x, s));
+    tick(h, GBPROP_PHASE_COMBINE);
     GB_LAUNCH(launch_step_end(h->d_ctrl, s));
+    tick(h, GBPROP_PHASE_OTHER);
     return GBPROP_OK;
 }
 
@@ -705,6 +741,39 @@ gbprop_status ensure_graph(gbprop_ctx* h) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
     return GBPROP_OK;
+}
+
+// Device-side failures (pamp.h:544-550 throws on a singular Pade denominator; here the kernels
+// record the failure in the handle's Ctrl flags and carry on without hanging).  After each
+// advance the three flags are copied to pinned host memory behind an event; device_errors
+// reads them once that event has completed -- without waiting (block = false: a failure is
+// reported by the first call after the GPU has finished the failing step) or after waiting
+// for it (block = true: synchronize, advance_host, get_stats).  A reported failure is cleared
+// on the device so that the handle can be used again.
+gbprop_status arm_flags(gbprop_ctx* h) {
+    GB_CUDA(cudaMemcpyAsync(h->h_flags, &h->d_ctrl->lu_info, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA(cudaEventRecord(h->ev_flags, h->stream));
+    h->flags_armed = true;
+    return GBPROP_OK;
+}
+
+gbprop_status report_flags(gbprop_ctx* h, int lu, int nonfinite, int timeout) {
+    if (!lu && !nonfinite && !timeout) return GBPROP_OK;
+    GB_CUDA(cudaMemsetAsync(&h->d_ctrl->lu_info, 0, 3 * sizeof(int), h->stream));
+    // the first cause: a wait that gave up leaves stale data, a non-finite vector makes the
+    // Pade denominator non-finite too
+    if (timeout) return fail(GBPROP_ETIMEOUT, "a bounded device-side wait gave up (bulk-copy staging or grid barrier)");
+    if (nonfinite) return fail(GBPROP_ENONFINITE, "non-finite Krylov norm or Hessenberg matrix");
+    return fail(GBPROP_ELU, "Pade denominator singular (LU info " + std::to_string(lu) + ")");
+}
+
+gbprop_status device_errors(gbprop_ctx* h, bool block) {
+    if (!h->flags_armed) return GBPROP_OK;
+    cudaError_t e = block ? cudaEventSynchronize(h->ev_flags) : cudaEventQuery(h->ev_flags);
+    if (e == cudaErrorNotReady) return GBPROP_OK;
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("flag event: ") + cudaGetErrorString(e));
+    h->flags_armed = false;
+    return report_flags(h, h->h_flags[0], h->h_flags[1], h->h_flags[2]);
 }
 
 gbprop_status ensure_sched(gbprop_ctx* h, int n) {
@@ -752,6 +821,8 @@ gbprop_status gbprop_create(gbprop_handle* out, int nl, int nr, int precision, i
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_flags, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_flags, 3 * sizeof(int));
     if (e != cudaSuccess) {
         delete h;
         return fail(GBPROP_ECUDA, std::string("stream/event creation: ") + cudaGetErrorString(e));
@@ -918,6 +989,7 @@ gbprop_status gbprop_advance(gbprop_handle h, void* psi, int nsteps, const doubl
     if (nsteps == 0) return GBPROP_OK;
     if (!scalings) return fail(GBPROP_EINVAL, "null scaling schedule");
     gbprop_status st;
+    if ((st = device_errors(h, false))) return st;      // a failure of an earlier call, if known by now
     GB_CUDA(h->begin());
     if ((st = enqueue_enter(h, psi, h->stream))) return st;
     // steps are issued in chunks of the schedule capacity
@@ -938,6 +1010,7 @@ gbprop_status gbprop_advance(gbprop_handle h, void* psi, int nsteps, const doubl
         done += chunk;
     }
     if ((st = enqueue_leave(h, psi, h->stream))) return st;
+    if ((st = arm_flags(h))) return st;
     GB_CUDA(h->end());
     return GBPROP_OK;
 }
@@ -957,7 +1030,7 @@ gbprop_status gbprop_advance_host(gbprop_handle h, void* psi_host, int nsteps, c
     if (st) return st;
     GB_CUDA(cudaMemcpyAsync(psi_host, d, bytes, cudaMemcpyDeviceToHost, h->ustream));
     GB_CUDA(cudaStreamSynchronize(h->ustream));
-    return GBPROP_OK;
+    return device_errors(h, true);
 }
 
 gbprop_status gbprop_matvec(gbprop_handle h, const void* src, void* dst, double scaling, int balanced) {
@@ -1013,16 +1086,17 @@ gbprop_status gbprop_get_stats(gbprop_handle h, gbprop_stats* out) {
     out->last_basis_size = c.nbasis;
     out->last_scaling_order = c.scaling_order;
     out->error_estimate = c.err_est;
-    if (c.lu_info) return fail(GBPROP_ELU, "Pade denominator singular (LU info " + std::to_string(c.lu_info) + ")");
-    if (c.nonfinite) return fail(GBPROP_ENONFINITE, "non-finite Krylov norm");
-    if (c.wait_timeout) return fail(GBPROP_ETIMEOUT, "a bounded device wait gave up (solve table staging)");
-    return GBPROP_OK;
+    h->flags_armed = false;                             // the copy above is newer than any armed one
+    return report_flags(h, c.lu_info, c.nonfinite, c.wait_timeout);
 }
 
 gbprop_status gbprop_reset_stats(gbprop_handle h) {
     if (gbprop_status st = check_handle(h, true)) return st;
-    GB_CUDA(cudaMemsetAsync(h->d_ctrl, 0, sizeof(Ctrl), h->stream));
+    // counters and error flags only: the host-set fields (wait_limit, inject_lu) stay
+    GB_CUDA(cudaMemsetAsync(h->d_ctrl, 0, offsetof(Ctrl, inject_lu), h->stream));
+    GB_CUDA(cudaMemsetAsync(&h->d_ctrl->ro_go, 0, sizeof(Ctrl) - offsetof(Ctrl, ro_go), h->stream));
     GB_CUDA(cudaStreamSynchronize(h->stream));
+    h->flags_armed = false;
     return GBPROP_OK;
 }
 
@@ -1038,6 +1112,62 @@ gbprop_status gbprop_synchronize(gbprop_handle h) {
     if (gbprop_status st = check_handle(h, false)) return st;
     GB_CUDA(cudaStreamSynchronize(h->stream));
     GB_CUDA(cudaStreamSynchronize(h->ustream));
+    return device_errors(h, true);
+}
+
+gbprop_status gbprop_time_step(gbprop_handle h, void* psi, double scaling, double dt_re, double dt_im,
+                               gbprop_step_timers* out) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!psi || !out) return fail(GBPROP_EINVAL, "null argument");
+    if (gbprop_status st = device_errors(h, false)) return st;
+    if (h->tick_pool.empty()) {
+        h->tick_pool.resize(4 * kMaxBasis * 8 + 64, nullptr);
+        for (cudaEvent_t& e : h->tick_pool) GB_CUDA(cudaEventCreate(&e));
+    }
+    gbprop_status st;
+    if ((st = ensure_sched(h, 1))) return st;
+    SchedEntry se = {scaling, dt_re, dt_im};
+    GB_CUDA(h->begin());
+    GB_CUDA(cudaMemcpyAsync(h->d_sched, &se, sizeof(se), cudaMemcpyHostToDevice, h->stream));
+    GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), h->stream));
+    std::vector<std::pair<int, cudaEvent_t>> ticks;
+    cudaEvent_t start = h->tick_pool.back();
+    GB_CUDA(cudaEventRecord(start, h->stream));
+    h->timing = &ticks;
+    const long long before = launch_count();
+    st = enqueue_enter(h, psi, h->stream);
+    if (!st) st = enqueue_step(h);
+    if (!st) st = enqueue_leave(h, psi, h->stream);
+    h->timing = nullptr;
+    if (st) return st;
+    if ((st = arm_flags(h))) return st;
+    GB_CUDA(h->end());
+    GB_CUDA(cudaStreamSynchronize(h->stream));
+    std::memset(out, 0, sizeof(*out));
+    out->launches = launch_count() - before;
+    cudaEvent_t prev = start;
+    for (const auto& t : ticks) {
+        float ms = 0.f;
+        GB_CUDA(cudaEventElapsedTime(&ms, prev, t.second));
+        out->ms[t.first] += ms;
+        out->count[t.first] += 1;
+        out->total_ms += ms;
+        prev = t.second;
+    }
+    return device_errors(h, true);
+}
+
+gbprop_status gbprop_debug_set(gbprop_handle h, int key, long long value) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (key == GBPROP_DEBUG_WAIT_LIMIT) {
+        GB_CUDA(cudaMemcpyAsync(&h->d_ctrl->wait_limit, &value, sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+    } else if (key == GBPROP_DEBUG_INJECT_LU) {
+        const int v = value ? 1 : 0;
+        GB_CUDA(cudaMemcpyAsync(&h->d_ctrl->inject_lu, &v, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    } else {
+        return fail(GBPROP_EINVAL, "unknown debug key");
+    }
+    GB_CUDA(cudaStreamSynchronize(h->stream));
     return GBPROP_OK;
 }
 
@@ -1290,8 +1420,7 @@ extern "C" gbprop_status gbprop_expokit_advance(gbprop_handle h, void* psi, int 
             GB_CUDA(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
             GB_CUDA(cudaMemcpyAsync(Hd.data(), h->d_H, Hd.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
             GB_CUDA(cudaStreamSynchronize(h->stream));
-            if (c.nonfinite) return fail(GBPROP_ENONFINITE, "non-finite Krylov norm");
-            if (c.wait_timeout) return fail(GBPROP_ETIMEOUT, "a bounded device wait gave up");
+            if (c.nonfinite || c.wait_timeout) return report_flags(h, 0, c.nonfinite, c.wait_timeout);
             const double beta = c.beta0;
             if (vnorm < 0.0) vnorm = beta;
             acc.hump = std::max(acc.hump, beta / vnorm);
@@ -1397,6 +1526,12 @@ struct gbprop_batch_ctx {
     cudaGraphExec_t g[4] = {nullptr, nullptr, nullptr, nullptr};
     long long g_launches[4] = {0, 0, 0, 0};
     std::vector<void*> graph_psi;
+    // members' error flags gathered after each advance (see launch_gather_flags)
+    Ctrl** d_ctrls = nullptr;
+    int* d_flags = nullptr;
+    int* h_flags = nullptr;
+    cudaEvent_t ev_flags = nullptr;
+    bool flags_armed = false;
     ~gbprop_batch_ctx() {
         for (cudaGraphExec_t x : g)
             if (x) cudaGraphExecDestroy(x);
@@ -1404,6 +1539,10 @@ struct gbprop_batch_ctx {
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_in) cudaEventDestroy(ev_in);
         if (ev_out) cudaEventDestroy(ev_out);
+        if (ev_flags) cudaEventDestroy(ev_flags);
+        if (h_flags) cudaFreeHost(h_flags);
+        if (d_ctrls) cudaFree(d_ctrls);
+        if (d_flags) cudaFree(d_flags);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -1450,6 +1589,26 @@ gbprop_status batch_capture(gbprop_batch b, void* const* psi, int what, cudaGrap
     return GBPROP_OK;
 }
 
+// The members' error flags (see device_errors), gathered into one pinned copy per advance.
+gbprop_status batch_errors(gbprop_batch b, bool block) {
+    if (!b->flags_armed) return GBPROP_OK;
+    cudaError_t e = block ? cudaEventSynchronize(b->ev_flags) : cudaEventQuery(b->ev_flags);
+    if (e == cudaErrorNotReady) return GBPROP_OK;
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("flag event: ") + cudaGetErrorString(e));
+    b->flags_armed = false;
+    const int p = b->h_flags[3] - 1;
+    if (p < 0 || p >= (int)b->hs.size()) return GBPROP_OK;
+    gbprop_ctx* h = b->hs[p];
+    // clear every member's flags (only members with a failure have any set)
+    for (gbprop_ctx* x : b->hs) GB_CUDA(cudaMemsetAsync(&x->d_ctrl->lu_info, 0, 3 * sizeof(int), b->stream));
+    cudaStream_t keep = h->stream;
+    h->stream = b->stream;
+    gbprop_status st = report_flags(h, b->h_flags[0], b->h_flags[1], b->h_flags[2]);
+    h->stream = keep;
+    set_last_error((std::string(gbprop_last_error()) + " (problem " + std::to_string(p) + " of the batch)").c_str());
+    return st;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1474,6 +1633,15 @@ gbprop_status gbprop_batch_create(gbprop_batch* out, const gbprop_handle* proble
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming);
     b->ev_join.assign(count, nullptr);
     for (int p = 0; p < count && e == cudaSuccess; ++p) e = cudaEventCreateWithFlags(&b->ev_join[p], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_flags, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_flags, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_flags, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_ctrls, count * sizeof(Ctrl*));
+    if (e == cudaSuccess) {
+        std::vector<Ctrl*> cs(count);
+        for (int p = 0; p < count; ++p) cs[p] = problems[p]->d_ctrl;
+        e = cudaMemcpy(b->d_ctrls, cs.data(), count * sizeof(Ctrl*), cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess) {
         delete b;
         return fail(GBPROP_ECUDA, std::string("batch stream/event creation: ") + cudaGetErrorString(e));
@@ -1503,6 +1671,7 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
     const size_t P = b->hs.size();
     for (size_t p = 0; p < P; ++p)
         if (!psi[p]) return fail(GBPROP_EINVAL, "null wavefunction in batch");
+    if (gbprop_status st = batch_errors(b, false)) return st;
     GB_CUDA(cudaEventRecord(b->ev_in, b->ustream));
     GB_CUDA(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
     static const int kShape[4] = {1 | 2 | 4, 1 | 2, 2, 2 | 4};
@@ -1553,9 +1722,20 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
         }
         done += chunk;
     }
+    GB_LAUNCH(launch_gather_flags(b->d_ctrls, (int)P, b->d_flags, b->stream));
+    GB_CUDA(cudaMemcpyAsync(b->h_flags, b->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    GB_CUDA(cudaEventRecord(b->ev_flags, b->stream));
+    b->flags_armed = true;
     GB_CUDA(cudaEventRecord(b->ev_out, b->stream));
     GB_CUDA(cudaStreamWaitEvent(b->ustream, b->ev_out, 0));
     return GBPROP_OK;
+}
+
+gbprop_status gbprop_batch_synchronize(gbprop_batch b) {
+    if (!b) return fail(GBPROP_EINVAL, "null batch");
+    GB_CUDA(cudaStreamSynchronize(b->stream));
+    GB_CUDA(cudaStreamSynchronize(b->ustream));
+    return batch_errors(b, true);
 }
 
 gbprop_status gbprop_batch_destroy(gbprop_batch b) {

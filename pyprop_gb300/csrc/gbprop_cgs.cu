@@ -25,8 +25,8 @@ constexpr long kBarrierSpinLimit = 1L << 24;   // polls (each an L2 round trip) 
 // (zeroed before the step's first launch): barrier number t of the step completes when the
 // counter reaches (t + 1) * nblocks.  One acquire-release atomic per CTA and acquire polls
 // (1.2 us per barrier over 152 CTAs, against 2.3 us with full fences around a volatile
-// sense flag).  Bounded: after kBarrierSpinLimit polls it records ctrl->wait_timeout and
-// returns false.
+// sense flag).  Bounded: after kBarrierSpinLimit polls (or the handle's Ctrl::wait_limit, see
+// wait_budget) it records ctrl->wait_timeout and returns false.
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -41,9 +41,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, un
         unsigned old;
         asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(bar) : "memory");
         const unsigned target = (t + 1) * nblocks;
+        const long lim = wait_budget(ctrl, kBarrierSpinLimit);
         long it = 0;
         while ((int)(ld_acquire_gpu(bar) - target) < 0) {
-            if (++it > kBarrierSpinLimit) {
+            if (++it > lim) {
                 ctrl->wait_timeout = 1;
                 ok = 0;
                 break;
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
             if (v0s) bulk_g2s(c0, v0s + i0, 2 * row, &s_bar);
             for (int k = k_first; k < nv; ++k) bulk_g2s(cache + (size_t)k * chunk, V + (size_t)k * n + i0, row, &s_bar);
         }
-        if (!__syncthreads_and(mbar_wait0(&s_bar))) {
+        if (!__syncthreads_and(mbar_wait0(&s_bar, wait_budget(ctrl, kInvWaitLimit)))) {
             if (tid == 0) ctrl->wait_timeout = 1;
             mbar_wait0(&s_bar);                      // copies in flight land before exit
             return;

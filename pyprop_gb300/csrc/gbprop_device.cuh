@@ -96,6 +96,15 @@ __device__ __forceinline__ void set_inv_beta(Ctrl* c, double beta) {
 // ---------------------------------------------------------------------------
 constexpr long kInvWaitLimit = 1L << 24;      // try_wait polls before a staging wait gives up
 
+// Poll budget of the first bounded wait of a launch (the staging wait, the grid barrier):
+// the handle's Ctrl::wait_limit when set (> 0), none when negative (a test makes the wait
+// give up at once), else `dflt`.  Waits that only drain copies in flight before an early
+// exit keep the fixed default, so a CTA never leaves with bulk copies still landing.
+__device__ __forceinline__ long wait_budget(const Ctrl* ctrl, long dflt) {
+    const long long v = ctrl ? ctrl->wait_limit : 0;
+    return v == 0 ? dflt : (v < 0 ? 0L : (long)v);
+}
+
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
@@ -107,9 +116,9 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
 }
 
 // Bounded wait for phase 0 of the mbarrier; false when the poll limit was reached.
-__device__ __forceinline__ bool mbar_wait0(unsigned long long* bar) {
+__device__ __forceinline__ bool mbar_wait0(unsigned long long* bar, long limit = kInvWaitLimit) {
     const unsigned a = smem_u32(bar);
-    for (long it = 0; it < kInvWaitLimit; ++it) {
+    for (long it = 0; it < limit; ++it) {
         unsigned done;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
                      " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(a) : "memory");

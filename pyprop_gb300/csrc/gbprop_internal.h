@@ -108,15 +108,19 @@ template <typename T> struct BandOp {
     const T* slots_lo;       // FP32 only: slot - (float)slot, the coefficients' rounding remainder
 };
 
-// Device control block of one handle; every field is written by kernels only.
+// Device control block of one handle.  Every field is written by kernels only, except
+// inject_lu and wait_limit (set by the host through gbprop_debug_set).
 struct Ctrl {
     int step;               // index of the current entry of the schedule array
     int broken;             // happy breakdown seen in the current step
     int nbasis;             // Krylov vectors built in the current step
-    int lu_info;            // last non-zero LU info of the Pade solve
     int scaling_order;      // s of the last scaling-and-squaring
+    // error flags (sticky until the host reports them; kept adjacent: copied and cleared as one)
+    int lu_info;            // last non-zero LU info of the Pade solve
     int nonfinite;          // a NaN/Inf norm was seen
-    int wait_timeout;       // a bounded device-side wait (shared-memory staging) gave up
+    int wait_timeout;       // a bounded device-side wait (bulk-copy staging, grid barrier) gave up
+    int inject_lu;          // test hook: the next exponentials report a zero pivot (host-set)
+    long long wait_limit;   // polls of a launch's first bounded wait: 0 = default, < 0 = give up at once
     int ro_go;              // re-orthogonalisation requested for the current vector
     int ro_count;           // re-orthogonalisation passes done for the current vector
     long long operator_count;
@@ -224,6 +228,9 @@ bool expm_df_single_fits(int m);
 cudaError_t launch_combine(int prec, const void* V, const double2* v0, long n, const Ctrl* ctrl, void* out,
                            cudaStream_t s);
 cudaError_t launch_step_end(Ctrl* ctrl, cudaStream_t s);
+// out[0..2] = max of the members' (lu_info, nonfinite, wait_timeout); out[3] = 1 + the first
+// member with any of them set (0 if none).  One CTA.
+cudaError_t launch_gather_flags(Ctrl* const* ctrls, int count, int* out, cudaStream_t s);
 cudaError_t launch_tensor_multiply_ref(int storage, const double2* V, int npairs, const int* pairs, int kb,
                                        double scaling, const double2* src, double2* dst, int nl, int nr,
                                        cudaStream_t s);

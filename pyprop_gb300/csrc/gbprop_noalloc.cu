@@ -1,10 +1,10 @@
 // Allocation-free variant of the Arnoldi block inner product.
 //
 // Some callers cannot allocate device memory at the point where they need
-// the block inner product: code running while a CUDA graph is being captured
-// (cudaMalloc is not a capturable operation), custom allocators or memory
-// pools that call back into this library, and embedded hosts that hand the
-// library only fixed buffers.  gbprop_block_inner_product asks its caller
+// the block inner product: custom allocators or memory pools that call back
+// into this library (allocating there would re-enter the allocator), and
+// embedded or real-time hosts that hand the library only fixed buffers and
+// allow no allocation after start-up.  gbprop_block_inner_product asks its caller
 // for a workspace; this entry point instead uses the fixed scratch array
 // below, so it calls no cudaMalloc, cudaFree or allocating library routine.
 //

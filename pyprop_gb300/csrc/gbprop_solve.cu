@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
             }
         }
         bool ok = true;
-        if (STAGE) ok = mbar_wait0(&s_bar);
+        if (STAGE) ok = mbar_wait0(&s_bar, wait_budget(ctrl, kInvWaitLimit));
         if (!__syncthreads_and(ok)) {
             if (tid == 0) ctrl->wait_timeout = 1;
             if (STAGE) mbar_wait0(&s_bar);
@@ -757,7 +757,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
         }
     }
     bool ok = true;
-    if (STAGE) ok = mbar_wait0(&s_bar);
+    if (STAGE) ok = mbar_wait0(&s_bar, wait_budget(ctrl, kInvWaitLimit));
     if (!__syncthreads_and(ok)) {
         if (tid == 0) ctrl->wait_timeout = 1;
         if (STAGE) mbar_wait0(&s_bar);             // let copies in flight land before exit

@@ -401,3 +401,25 @@ def test_block_inner_product_stateless(prec, n, nv):
     st = L.gbprop_block_inner_product(prec, _native.ptr(dV), n, nv, _native.ptr(dw), 0, _native.ptr(out),
                                       _native.ptr(work), ws - 1, None)
     assert st == 1
+
+
+def test_time_step_phases(small):
+    """gbprop_time_step (per-phase timers, one step outside the graph) does the same arithmetic
+    as one gbprop_advance step and tags every launch with its phase."""
+    import torch
+    h = small.Propagator.Handle()
+    m = small.Propagator.BasisSize
+    psi0 = small.psi.GetDataNumpy().copy()
+    scal = scalings_for(small, 1)
+    a = _dev(psi0)
+    h.advance(a, scal, small.TimeStep)
+    b = _dev(psi0)
+    t = h.time_step(b, float(scal[0]), small.TimeStep)
+    torch.cuda.synchronize()
+    assert rel(_host(b), _host(a)) < 1e-15
+    assert t["band"][1] == m                      # one band launch per matvec
+    assert t["solve"][1] == 2 * m + 1             # U^-1 and U^-T per matvec, U^-1 x at the end
+    assert t["exponential"][1] == 1 and t["combine"][1] == 1
+    assert t["gram_schmidt"][1] >= m + 1          # ||x|| and one or more launches per Arnoldi step
+    assert t["launches"] == sum(v[1] for k, v in t.items() if isinstance(v, tuple))
+    assert abs(t["total_ms"] - sum(v[0] for k, v in t.items() if isinstance(v, tuple))) < 1e-9
