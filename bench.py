@@ -37,9 +37,16 @@ FALLBACK_HBM_GBS = 6800.0
 # FMA issue rates measured on GB300 with dependency-free FMA loops over all SMs
 FP64_PEAK_TFLOPS = 1.195
 FP32_PEAK_TFLOPS = 69.9
-# DRAM bytes (read + write) per launch of the band kernel on the large workload, from one
-# ncu capture each (profiles/band_kernel_hydrogen_large.md)
-BAND_TRAFFIC = {"fp64": 20802560, "fp32-mixed": 20300288}
+# DRAM bytes (read + write) per launch of each step phase's kernel on the large workload,
+# from one ncu capture of that kernel (capture constants, not measured by this run; the
+# capture each comes from is named in PHASE_TRAFFIC_SOURCE)
+PHASE_TRAFFIC = {
+    ("fp64", "band"): 20802560, ("fp32-mixed", "band"): 20300288,
+}
+PHASE_TRAFFIC_SOURCE = {
+    "band": "profiles/band_kernel_hydrogen_large.md (ncu --set full, one launch)",
+}
+GOLD_LARGE = os.path.join(ROOT, "tests", "golden", "oracle_large.npz")
 
 
 def _dist():
@@ -175,6 +182,62 @@ def coef_bytes_of(prob, precision):
     w = inverse_band_width(prob)
     solve = 2 * ((w + 1) * nr * 4 + (kd + 1) * nr * 8)
     return band, solve, w
+
+
+def phase_bytes(N, nr, m, s, band_coef, solve_tab, state_elem):
+    """Algorithmic bytes of one step per phase (each array read or written once per launch):
+      solve         m U^-1 launches: read r, write U^-1 r and the basis row v_J (3 N s) + tables;
+                    m U^-T launches: read, write (2 N s) + tables; the state transform U^-1 x:
+                    read x (16 N), write psi (N state_elem) + tables
+      band          m launches: read the source, write the result (2 N s) + the band slots
+      gram_schmidt  launch J reads v_0..v_J and w, writes w: (J + 3) N s; plus ||x|| (16 N)
+      combine       read the m basis rows, read and write x (FP64): m N s + 32 N
+      other         x = U psi: read psi, write x (FP64)
+    solve_tab = bytes of one solve's tables (approximate-inverse band FP32 + factor diagonals)."""
+    return {
+        "solve": m * (3 * N * s + solve_tab) + m * (2 * N * s + solve_tab) + (16 * N + N * state_elem + solve_tab),
+        "band": m * (2 * N * s + band_coef),
+        "gram_schmidt": sum((J + 3) * N * s for J in range(m)) + 16 * N,
+        "exponential": 0,
+        "combine": m * N * s + 32 * N,
+        "other": N * state_elem + 16 * N,
+    }
+
+
+def phase_roofline(h, psi_dev, scaling, dt, N, nr, m, elem, band_coef, solve_coef, precision, peak, peak_kind,
+                   reps=5):
+    """Per-phase times of the step (gbprop_time_step: one step outside its graph, an event after
+    every launch, averaged over `reps` steps after one warm-up) against each phase's algorithmic
+    bytes; the roofline entry of the line is the phase with the largest share of the step."""
+    h.time_step(psi_dev, scaling, dt)
+    acc = None
+    for _ in range(reps):
+        t = h.time_step(psi_dev, scaling, dt)
+        if acc is None:
+            acc = {k: [v[0], v[1]] for k, v in t.items() if isinstance(v, tuple)}
+            acc["total_ms"] = t["total_ms"]
+        else:
+            for k, v in t.items():
+                if isinstance(v, tuple):
+                    acc[k][0] += v[0]
+            acc["total_ms"] += t["total_ms"]
+    total = acc.pop("total_ms") / reps
+    pb = phase_bytes(N, nr, m, elem, band_coef, solve_coef // 2, elem)
+    per = {}
+    for name, (ms, cnt) in acc.items():
+        ms /= reps
+        b = pb[name]
+        ent = {"ms_per_step": ms, "share": ms / total if total else 0.0, "launches_per_step": cnt,
+               "algorithmic_bytes_per_step": b}
+        if b and ms > 0:
+            ach = b / (ms * 1e-3) / 1e9
+            ent.update({"achieved": ach, "frac": ach / peak})
+        tr = PHASE_TRAFFIC.get((precision, name))
+        if tr is not None and cnt:
+            ent["traffic_per_launch_capture"] = tr
+        per[name] = ent
+    top = max(per, key=lambda k: per[k]["ms_per_step"])
+    return top, per, total
 
 
 def build_problem(workload, precision, device):
@@ -555,7 +618,7 @@ def main():
     if args.precision == "fp64" and not args.no_mixed:
         mixed = measure_single(args, "fp32-mixed", device, world, with_e2e=True)["line"]
         line["fp32_mixed"] = {k: mixed[k] for k in ("value", "unit", "ms_per_step", "e2e", "roofline", "matvec_ms",
-                                                    "gpu_launches")}
+                                                    "gpu_launches", "parity_vs_oracle") if k in mixed}
         line["fp32_mixed"]["speedup_vs_fp64"] = mixed["value"] / line["value"]
         line["fp32_mixed"]["dtype"] = mixed["dtype"]
     if not args.no_precision_report:
@@ -652,6 +715,10 @@ def measure_single(args, precision, device, world, with_e2e=True):
         else:
             t_band = e0.elapsed_time(e1) / reps
     peak, peak_kind = load_peaks()
+    # per-phase roofline of the step (events between launches, outside the graph)
+    scal0 = bp._scaling(prob.PropagatedTime)
+    top, per_phase, phase_total = phase_roofline(h, src.clone(), scal0, dt, N, nr, m, elem, band_coef, solve_coef,
+                                                 precision, peak, peak_kind)
     band_bytes = 2 * N * elem + band_coef
     achieved = band_bytes / (t_band * 1e-3) / 1e9
     _, nterms = operator_slots(prob)
@@ -667,13 +734,29 @@ def measure_single(args, precision, device, world, with_e2e=True):
         compute = {"unit": "TFLOP/s", "achieved": band_flops / (t_band * 1e-3) / 1e12, "peak": FP32_PEAK_TFLOPS,
                    "peak_source": "measured FP32 FMA issue rate on GB300", "what": "FP32 ops of the compensated sums"}
     compute["frac"] = compute["achieved"] / compute["peak"]
+    kernels = {"solve": "k_solve_inv (overlap-factor solves U^-1, U^-T)" if precision == "fp64" else
+               "k_solve_mixed / k_solve_inv (complex64 basis solves, FP64 state solve)",
+               "band": "k_band_apply (TensorPotentialMultiply, all terms)",
+               "gram_schmidt": "k_arnoldi_cgs (cooperative Gram-Schmidt) + k_norm",
+               "exponential": "k_expm_cluster (Pade scaling-and-squaring)",
+               "combine": "k_combine", "other": "k_tbmv + step bookkeeping"}
+    tp = per_phase[top]
+    launches_top = max(1, tp["launches_per_step"])
     roofline = {
-        "bound": "hbm", "kernel": "k_band_apply<%s> (TensorPotentialMultiply, all terms)" %
-                                  ("double" if precision == "fp64" else "float, hi/lo compensated"),
-        "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-        "traffic": BAND_TRAFFIC.get(precision), "launch_ms": t_band,
-        "algorithmic_bytes_per_launch": band_bytes,
-        "compute": compute,
+        "bound": "hbm", "kernel": kernels[top], "phase": top,
+        "achieved": tp.get("achieved"), "peak": peak, "unit": "GB/s", "frac": tp.get("frac"),
+        "peak_source": peak_kind,
+        "traffic": PHASE_TRAFFIC.get((precision, top)),
+        "traffic_source": PHASE_TRAFFIC_SOURCE.get(top) if (precision, top) in PHASE_TRAFFIC else None,
+        "launch_ms": tp["ms_per_step"] / launches_top,
+        "algorithmic_bytes_per_launch": tp["algorithmic_bytes_per_step"] / launches_top,
+        "how": "gbprop_time_step: one step outside its CUDA graph with an event after every launch (5 steps "
+               "averaged); achieved = the phase's algorithmic bytes per step / its time per step",
+        "step_ms_events": phase_total,
+        "per_phase": per_phase,
+        "band_kernel_alone": {"achieved": achieved, "frac": achieved / peak, "launch_ms": t_band,
+                              "algorithmic_bytes_per_launch": band_bytes,
+                              "traffic": PHASE_TRAFFIC.get((precision, "band")), "compute": compute},
     }
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -692,9 +775,36 @@ def measure_single(args, precision, device, world, with_e2e=True):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    par = parity_vs_fixture(args.workload, h, precision)
+    if par is not None:
+        line["parity_vs_oracle"] = par
     del h, prob
     torch.cuda.synchronize()
     return {"line": line}
+
+
+def parity_vs_fixture(workload, h, precision, nsteps=200):
+    """The workload against the oracle's states (tests/golden/oracle_large.npz, same coefficients
+    and field values), after the timed region: `nsteps` steps from the hydrogen ground state (a
+    smooth map; bar 1e-11 for FP64), and one step from the configured random start, whose stiff
+    modes make the step amplify rounding ~1e4-fold (reported beside the oracle's own response to
+    a 1e-16 relative change of the start)."""
+    if workload != "large" or not os.path.exists(GOLD_LARGE):
+        return None
+    import torch
+    g = np.load(GOLD_LARGE)
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    out = {"against": "oracle states (tests/golden/oracle_large.npz)"}
+    for start, key, n, name in (("gs0", "gs%d" % nsteps, nsteps, "ground_state"), ("psi0", "rand1", 1, "random_start")):
+        d = torch.as_tensor(g[start]).to("cuda", cdt)
+        h.advance(d, g["scalings"][:n], complex(g["dt"]))
+        h.synchronize()
+        got = d.cpu().numpy().astype(np.complex128)
+        want = g[key]
+        out[name] = {"steps": n, "rel_l2": float(np.linalg.norm(got - want) / np.linalg.norm(want))}
+    out["ground_state"]["bar"] = 1e-11 if precision == "fp64" else None
+    out["random_start"]["oracle_sensitivity_1e-16"] = float(g["sens1"])
+    return out
 
 
 def precision_report(device, nsteps=500):

@@ -127,6 +127,7 @@ class AdjointPropagator:
         torch = self.torch
         s = self.scalings(samples)
         psi = torch.as_tensor(np.ascontiguousarray(psi0)).to(self.device, self.cdt).clone()
+        # a new dict per call: a caller holding the previous call's tape keeps its checkpoints
         self._ckpt = {}
         self._s = s
         for n0 in range(0, self.nsteps, self.checkpoint):
@@ -149,9 +150,16 @@ class AdjointPropagator:
         return float(self.populations(psi, states)[0].sum())
 
     # -- adjoint ----------------------------------------------------------------
-    def gradient(self, psi_T, states):
-        """dO/dc_k for O = sum_b |<phi_b|S|psi_T>|^2 (after forward(keep=True))."""
+    def tape(self):
+        """The checkpoints and field values of the last forward(keep=True) call; pass it to
+        gradient() to differentiate that call after later forward calls."""
+        return (self._ckpt, self._s)
+
+    def gradient(self, psi_T, states, tape=None):
+        """dO/dc_k for O = sum_b |<phi_b|S|psi_T>|^2, for the forward call whose tape() is given
+        (default: the last forward(keep=True) call)."""
         torch = self.torch
+        ckpt, svals = tape if tape is not None else self.tape()
         nl, nr = self.problem.nl, self.problem.nr
         phi = torch.as_tensor(states).to(self.device, torch.complex128)
         Spsi = self._apply_S(psi_T).reshape(-1)
@@ -162,20 +170,20 @@ class AdjointPropagator:
         for n0 in reversed(range(0, self.nsteps, self.checkpoint)):
             n1 = min(self.nsteps, n0 + self.checkpoint)
             # recompute the forward states of this segment from its checkpoint
-            states_seg = [self._ckpt[n0].clone()]
-            psi = self._ckpt[n0].clone()
+            states_seg = [ckpt[n0].clone()]
+            psi = ckpt[n0].clone()
             for n in range(n0, n1 - 1):
-                self.h.advance(psi, self._s[n:n + 1], self.dt)
+                self.h.advance(psi, svals[n:n + 1], self.dt)
                 states_seg.append(psi.clone())
             for n in reversed(range(n0, n1)):
                 psi_n = states_seg[n - n0]
                 aug.zero_()
                 aug[nl:] = psi_n
-                self.h_aug.advance(aug, self._s[n:n + 1], self.dt)
+                self.h_aug.advance(aug, svals[n:n + 1], self.dt)
                 dpsi = aug[:nl]
                 dOds[n] = 2.0 * torch.sum(torch.conj(gamma.to(torch.complex128)) * self._apply_S(dpsi)).real
                 # co-state one step back: exp(+i dt A_n) in balanced coordinates
-                self.h.advance(gamma, self._s[n:n + 1], -self.dt)
+                self.h.advance(gamma, svals[n:n + 1], -self.dt)
         dOds = dOds.cpu().numpy()
         return self.W.T @ dOds, dOds
 
@@ -197,12 +205,14 @@ class ObservableFunction:
                 @staticmethod
                 def forward(ctx, samples, prop, psi0, states):
                     psi_T = prop.forward(psi0, samples.detach().cpu().numpy(), keep=True)
-                    ctx.prop, ctx.states, ctx.psi_T = prop, states, psi_T
+                    # this call's own checkpoints and field values: later forward calls through
+                    # the same propagator (several losses, line searches) do not disturb them
+                    ctx.prop, ctx.states, ctx.psi_T, ctx.tape = prop, states, psi_T, prop.tape()
                     return torch.tensor(prop.observable(psi_T, states), dtype=torch.float64)
 
                 @staticmethod
                 def backward(ctx, grad_out):
-                    g, _ = ctx.prop.gradient(ctx.psi_T, ctx.states)
+                    g, _ = ctx.prop.gradient(ctx.psi_T, ctx.states, tape=ctx.tape)
                     return torch.as_tensor(g, dtype=torch.float64) * grad_out, None, None, None
 
             ObservableFunction._impl = _F

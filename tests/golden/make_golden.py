@@ -25,7 +25,9 @@ with a stand-in for the compiled ReducedSphericalTools exposing GetSize() = LMax
 tests/golden/geometry_golden.npz; and the velocity-gauge pulse LaserFunctionVelocity of the
 helium_stabilization_sae example -> tests/golden/laser_golden.npz.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [REFERENCE_TREE]
+The reference tree (a checkout of pyprop) is the first argument, else the environment variable
+PYPROP_REFERENCE.
 """
 from __future__ import annotations
 
@@ -36,7 +38,14 @@ import types
 
 import numpy as np
 
-REF = "/root/reference"
+def _reference_tree():
+    path = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYPROP_REFERENCE", "")
+    if not path or not os.path.isdir(os.path.join(path, "pyprop")):
+        sys.exit("usage: make_golden.py REFERENCE_TREE (or set PYPROP_REFERENCE): a pyprop checkout")
+    return path
+
+
+REF = _reference_tree() if __name__ == "__main__" else None
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "setup_golden.npz")
 
 

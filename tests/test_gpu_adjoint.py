@@ -80,3 +80,23 @@ def test_autograd_function_backward():
     (3.0 * O).backward()
     g, _ = ap.gradient(ap.forward(psi0, c), states)
     assert rel(x.grad.numpy(), 3.0 * g) < 1e-13
+
+
+def test_autograd_two_forward_calls_then_backward_on_the_first():
+    """Two losses through one propagator: backward() of the first call uses that call's own
+    checkpoints and field values, not those of the later forward call."""
+    import torch
+    from pyprop_gb300.adjoint import ObservableFunction
+    _, states, psi0, c, ap = _setup()
+    c2 = 1.3 * c[::-1].copy()
+    x1 = torch.tensor(c, dtype=torch.float64, requires_grad=True)
+    x2 = torch.tensor(c2, dtype=torch.float64, requires_grad=True)
+    O1 = ObservableFunction.apply(x1, ap, psi0, states)
+    O2 = ObservableFunction.apply(x2, ap, psi0, states)
+    O1.backward()
+    O2.backward()
+    g1, _ = ap.gradient(ap.forward(psi0, c), states)
+    g2, _ = ap.gradient(ap.forward(psi0, c2), states)
+    assert rel(g1, g2) > 1e-3                       # the two calls have different gradients
+    assert rel(x1.grad.numpy(), g1) < 1e-13
+    assert rel(x2.grad.numpy(), g2) < 1e-13

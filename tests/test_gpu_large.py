@@ -1,0 +1,132 @@
+"""Parity on the benchmarked workload and on the largest problem size of the batch.
+
+Benchmarked workload (pyprop_gb300/configs/hydrogen_velocity_large.ini): hydrogen at scale,
+l = 0..63 x 1000 B-splines, pAMP m = 30, dt = 0.005, the whole 2000-step pulse, through the
+C ABI, against the oracle's states (tests/golden/oracle_large.npz, made by
+tests/golden/make_oracle_fixtures.py) on the same coefficients and field values:
+
+  * from the hydrogen ground state, where the step is a smooth map: states after 20, 200 and
+    2000 steps, bar 1e-11 relative L2 (FP64);
+  * from the configured seeded random start, whose random B-spline coefficients fill the
+    stiffest modes (||dt H_m|| ~ 2^17): there the unconverged m = 30 Krylov step amplifies any
+    rounding difference ~1e4-fold per step (the oracle's own response to a 1e-16 relative change
+    of the start is stored as sens1, sens2), so after a few steps the state depends on the
+    summation order for the reference's algorithm itself.  The GPU is compared after 1 and 2
+    steps within 30x that sensitivity.
+
+The FP32-mixed form is compared with the same FP64 states from the ground state.
+
+Batch-sized problem: l = 0..64 x 1500 B-splines, r_max = 400, m = 32 (the upper end of the
+batch's sizes), 20 steps from its ground state, alone and as a member of a batch (one-CTA
+exponential, fewest solve chunks), plus one step from its random start within 30x the oracle's
+sensitivity (tests/golden/oracle_batch_large.npz)."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+GOLD_LARGE = os.path.join(HERE, "golden", "oracle_large.npz")
+GOLD_BATCH = os.path.join(HERE, "golden", "oracle_batch_large.npz")
+
+FP64_TOL = 1e-11
+# complex64 Krylov basis and matvec from the ground state (the state is FP64 across the steps
+# of one call; measured on the small workload: 2.9e-7 after 500 steps)
+MIXED_TOL = 2e-6
+SENS_FACTOR = 30.0
+
+
+def _problem(precision):
+    import pyprop_gb300 as pp
+    conf = pp.Load(os.path.join(ROOT, "pyprop_gb300", "configs", "hydrogen_velocity_large.ini"))
+    conf.Propagation.Set("krylov_precision", precision)
+    prob = pp.Problem(conf)
+    prob.SetupStep()
+    return prob
+
+
+def _run(h, start, scal, dt, checkpoints, cdt):
+    import torch
+    d = torch.as_tensor(start).to("cuda", cdt)
+    out, done = {}, 0
+    for c in checkpoints:
+        h.advance(d, scal[done:c], dt)
+        h.synchronize()
+        out[c] = d.cpu().numpy().astype(np.complex128)
+        done = c
+    return out
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD_LARGE)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
+def test_benchmarked_workload_ground_state_vs_oracle(gold, precision):
+    import torch
+    prob = _problem(precision)
+    h = prob.Propagator.Handle()
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    got = _run(h, gold["gs0"], gold["scalings"], complex(gold["dt"]), (20, 200, 2000), cdt)
+    errs = {c: rel(x, gold["gs%d" % c]) for c, x in got.items()}
+    print(precision, "ground-state start, relative L2 vs oracle after 20/200/2000 steps:", errs)
+    assert h.stats().last_scaling_order == int(gold["gs_scaling_order"])
+    for c, e in errs.items():
+        assert e < (FP64_TOL if precision == "fp64" else MIXED_TOL), (c, e)
+
+
+def test_benchmarked_workload_random_start_vs_oracle(gold):
+    import torch
+    prob = _problem("fp64")
+    assert np.array_equal(prob.psi.GetDataNumpy().astype(np.complex128), gold["psi0"])   # the seeded start
+    h = prob.Propagator.Handle()
+    got = _run(h, gold["psi0"], gold["scalings"], complex(gold["dt"]), (1, 2), torch.complex128)
+    for c in (1, 2):
+        e, bar = rel(got[c], gold["rand%d" % c]), SENS_FACTOR * float(gold["sens%d" % c])
+        print("random start, %d step(s): %.3e (oracle sensitivity to a 1e-16 change: %.3e)" %
+              (c, e, float(gold["sens%d" % c])))
+        assert e < bar, (c, e, bar)
+    assert h.stats().last_scaling_order == int(gold["rand_scaling_order"])
+
+
+def _batch_problem():
+    from pyprop_gb300.batch import HydrogenProblem
+    return HydrogenProblem(lmax=64, nr=1500, rmax=400.0, m=32, dt=0.01, omega=0.04, e0=0.1, seed=20261206)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
+def test_batch_sized_problem_vs_oracle(precision):
+    import torch
+    from pyprop_gb300 import _native
+    from pyprop_gb300.batch import BatchPropagator, HydrogenProblem
+    g = np.load(GOLD_BATCH)
+    p = _batch_problem()
+    assert np.array_equal(p.initial_state(), g["psi0"])
+    prec = _native.FP64 if precision == "fp64" else _native.FP32_MIXED
+    tol = FP64_TOL if precision == "fp64" else MIXED_TOL
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    stream = torch.cuda.current_stream().cuda_stream
+    # alone (cluster exponential, solves spread over the GPU)
+    h = p.handle(prec, stream)
+    e_alone = rel(_run(h, g["gs0"], g["scalings"], p.dt, (20,), cdt)[20], g["gs20"])
+    if precision == "fp64":
+        e_rand = rel(_run(h, g["psi0"], g["scalings"], p.dt, (1,), cdt)[1], g["rand1"])
+        assert e_rand < SENS_FACTOR * float(g["sens1"]), (e_rand, float(g["sens1"]))
+    # inside a batch with two small problems (one-CTA exponential, fewest solve chunks)
+    others = [HydrogenProblem(lmax=3, nr=40, rmax=30.0, m=8, seed=s) for s in (5, 6)]
+    bp = BatchPropagator([p] + others, precision=prec, autotune=False)
+    bp.psi[0].copy_(torch.as_tensor(g["gs0"]).to(cdt))
+    scal = np.zeros((3, len(g["scalings"])))
+    scal[0] = g["scalings"]
+    bp.batch.advance(bp.psi, scal, [p.dt] + [o.dt for o in others])
+    bp.synchronize()
+    e_batch = rel(bp.psi[0].cpu().numpy().astype(np.complex128), g["gs20"])
+    print(precision, "batch-sized problem, 20 steps from the ground state: alone %.3e, in a batch %.3e" %
+          (e_alone, e_batch))
+    assert e_alone < tol and e_batch < tol

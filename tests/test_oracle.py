@@ -1,5 +1,7 @@
 """The CPU oracle against known answers: the reference's TestPade matrix, dense
 numpy/scipy algebra, and the reference's storage/layout conventions."""
+import os
+
 import numpy as np
 import pytest
 import scipy.linalg as sl
@@ -183,3 +185,22 @@ def test_happy_breakdown_eigenvector():
     assert st.breakdown_count == 1 and st.last_basis == 2
     want = psi * np.exp(-1j * 0.1 * diag)
     assert np.allclose(out, want, atol=1e-12)
+
+
+def test_oracle_reproduces_large_fixture():
+    """The oracle built on this host gives the committed states of the benchmarked workload
+    (l = 0..63 x 1000, m = 30): 20 steps from the ground state (a smooth map) and one step from
+    the seeded random start (a stiff one) within 30x the oracle's sensitivity to a 1e-16 change."""
+    import pyprop_gb300 as pp
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_large.npz"))
+    conf = pp.Load(os.path.join(os.path.dirname(__file__), "..", "pyprop_gb300", "configs",
+                                "hydrogen_velocity_large.ini"))
+    prob = pp.Problem(conf, device="cpu")
+    prob.SetupWavefunction()
+    assert np.array_equal(prob.psi.GetDataNumpy().astype(np.complex128), g["psi0"])
+    op = orc.Operator.from_problem(prob)
+    m, dt = int(g["m"]), complex(g["dt"])
+    psi, _ = op.advance(g["gs0"], m, dt, g["scalings"][:20])
+    assert np.linalg.norm(psi - g["gs20"]) / np.linalg.norm(g["gs20"]) < 1e-13
+    psi, _ = op.advance(g["psi0"], m, dt, g["scalings"][:1])
+    assert np.linalg.norm(psi - g["rand1"]) / np.linalg.norm(g["rand1"]) < 30 * float(g["sens1"])

@@ -1,8 +1,8 @@
 """The allocation-free block inner product against the workspace version.
 
 gbprop_block_inner_product_noalloc serves callers that cannot allocate device
-memory when they need the Arnoldi inner products (e.g. while a CUDA graph is
-being captured, or from inside a memory pool's callback): its reduction
+memory when they need the Arnoldi inner products (e.g. from inside a memory
+pool's callback, or a host that allows no allocation after start-up): its reduction
 scratch is a fixed array inside the library instead of a caller workspace.
 This file is collected last so that a failure here cannot hide any other
 test; it also passes on its own in a fresh process.
