@@ -94,8 +94,12 @@ gbprop_status gbprop_set_overlap(gbprop_handle h, int kd, const double* U_band);
  *   pairs          (npairs, 2) int32 (row, col); NULL for Diag/Ident
  *   kb             band half-width of the radial BandNH storage (order - 1)
  *   data           (npairs, (2kb+1)*nr) complex128 interleaved (PotentialData)
- *   time_dependent 1 if the potential is scaled by its time function
- * dest[row] += scaling * data[pair] * src[col]   (generator.py:352). */
+ *   time_dependent 0: static; k = 1..4: scaled by time function number k.  Every
+ *                  potential is scaled by its own time function f_k(t)
+ *                  (TensorPotential.py:98-100, looped in Propagator.py:61-66); potentials
+ *                  sharing one function share its number.  The handle's time-function
+ *                  count K is the largest number used (1 if none).
+ * dest[row] += f_k(t) * data[pair] * src[col]   (generator.py:352). */
 gbprop_status gbprop_add_potential(gbprop_handle h, int storage, int npairs, const int* pairs,
                                    int kb, const double* data, int time_dependent);
 
@@ -108,9 +112,11 @@ gbprop_status gbprop_finalize(gbprop_handle h);
  * (pampwrapper.cpp:84-108) for nsteps consecutive steps, on a DEVICE
  * wavefunction psi (complex128 for FP64, complex64 for FP32_MIXED), in place:
  *   psi <- U^-1 pAMP_m(U psi, dt; H(t_n))   for n = 0..nsteps-1
- * scalings[n] (HOST array) is the time function at the start of step n
- * (TensorPotential.py:98-100 with t = PropagatedTime).  dt may be complex
- * (imaginary time).  Asynchronous on the handle's stream.
+ * scalings (HOST array, nsteps x K, step-major) holds the K time functions at the
+ * start of each step: scalings[n*K + k-1] = f_k(t_n) (TensorPotential.py:98-100 with
+ * t = PropagatedTime; K = 1 for the reference's single-pulse configurations, where
+ * this is one value per step).  dt may be complex (imaginary time).  Asynchronous
+ * on the handle's stream.
  *
  * Failures on the device (the reference throws at once, pamp.h:544-550) are
  * returned as GBPROP_ELU (singular Pade denominator), GBPROP_ENONFINITE (NaN/Inf
@@ -130,8 +136,24 @@ gbprop_status gbprop_advance_host(gbprop_handle h, void* psi_host, int nsteps, c
 /* BasisPropagator.MultiplyHamiltonianBalancedOverlap (BasisPropagator.py:131-159)
  * when balanced != 0: dst = U^-H H(t) U^-1 src; otherwise
  * MultiplyHamiltonianNoOverlap (:126-129): dst = H(t) src.  DEVICE pointers of
- * the handle's precision; src is not modified. */
+ * the handle's precision; src is not modified.  gbprop_matvec scales every
+ * time-dependent potential by `scaling`; gbprop_matvec_scalings takes the K time
+ * functions' values (HOST array of K doubles). */
 gbprop_status gbprop_matvec(gbprop_handle h, const void* src, void* dst, double scaling, int balanced);
+gbprop_status gbprop_matvec_scalings(gbprop_handle h, const void* src, void* dst, const double* scalings,
+                                     int balanced);
+
+/* Problem.AdvanceStep's renormalization (Problem.py:167-168: psi.Normalize() after every
+ * step when the Propagation key renormalization is true; Wavefunction::Normalize,
+ * core/wavefunction.cpp:194-218): on != 0 makes every step of gbprop_advance and
+ * gbprop_expokit_advance end with psi <- psi / ||psi||_S, on the device. */
+gbprop_status gbprop_set_renormalization(gbprop_handle h, int on);
+
+/* Wavefunction::InnerProduct (core/wavefunction.cpp:207-218 -> CombinedRepresentation::
+ * InnerProduct, combinedrepresentation.cpp:423-474): out[0], out[1] = Re, Im of a^H (I x S) b
+ * for DEVICE wavefunctions a, b of the handle's precision, with S = U^T U the radial overlap
+ * (formed as (U a)^H (U b) in FP64).  Synchronous; the norm is sqrt(out[0]) for b = a. */
+gbprop_status gbprop_inner_product(gbprop_handle h, const void* a, const void* b, double* out);
 
 /* CombinedRepresentation::MultiplySqrtOverlap(false) / SolveSqrtOverlap(conj)
  * (combinedrepresentation.cpp:207-238), in place on a DEVICE wavefunction. */
@@ -168,7 +190,7 @@ typedef struct {
     double total_ms;
     long long launches;
 } gbprop_step_timers;
-gbprop_status gbprop_time_step(gbprop_handle h, void* psi, double scaling, double dt_re, double dt_im,
+gbprop_status gbprop_time_step(gbprop_handle h, void* psi, const double* scalings, double dt_re, double dt_im,
                                gbprop_step_timers* out);
 
 /* Test hooks for the failure paths, no counterpart in the reference (its failures are
@@ -199,8 +221,9 @@ typedef struct {
 /* ExpokitPropagator.AdvanceStep (pyprop/propagator/KrylovPropagator.py:44-49 ->
  * core/krylov/expokit/expokitpropagator.cpp:36-103 -> Expokit zgexpv): nsteps steps of size
  * |dt|, each psi <- U^-1 exp(-i |dt| A) U psi (imaginary dt: exp(-|dt| A)), A the balanced
- * operator at scalings[k] (fixed within step k, as the reference's callback fixes the step's
- * start time), evaluated by Krylov sub-steps with local error control.  The Krylov dimension
+ * operator at the time functions of step k (scalings as in gbprop_advance, fixed within the
+ * step, as the reference's callback fixes the step's start time), evaluated by Krylov
+ * sub-steps with local error control.  The Krylov dimension
  * is the handle's krylov_basis_size - 1 (a handle for Expokit holds m + 1 vectors); tol and
  * anorm are krylov_tolerance and krylov_norm.  stats may be NULL.  Host-driven (the sub-step
  * sizes depend on the error estimates); returns after the work is enqueued and the last
@@ -224,9 +247,11 @@ gbprop_status gbprop_autotune(gbprop_handle h, int* variant);
 typedef struct gbprop_batch_ctx* gbprop_batch;
 gbprop_status gbprop_batch_create(gbprop_batch* out, const gbprop_handle* problems, int count, int autotune,
                                   void* stream);
-/* psi[p]: DEVICE wavefunction of problem p; scalings: count x nsteps HOST array
- * (row p = time-function values of problem p at the start of each step);
- * dt: count x 2 HOST array (re, im of each problem's time step). */
+/* psi[p]: DEVICE wavefunction of problem p; scalings: HOST array of the problems'
+ * blocks one after another, problem p's block nsteps x K_p as in gbprop_advance
+ * (K_p = 1 for every problem: a count x nsteps array, row p = problem p's time
+ * function at the start of each step); dt: count x 2 HOST array (re, im of each
+ * problem's time step). */
 gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps, const double* scalings,
                                    const double* dt);
 /* Waits for the batch's work; returns a device-side failure of any member (see

@@ -223,20 +223,23 @@ typedef struct {
     const cplx* U;           /* overlap Cholesky factor, upper band storage (nr, kd+1) */
     int npot;
     const int* kind;         /* per potential: ORC_DIAG_BANDNH or ORC_SIMP_BANDNH */
-    const int* timedep;      /* per potential: 1 if scaled by the time function */
+    const int* timedep;      /* per potential: 0 static, k >= 1 scaled by time function k */
     const int* npairs;       /* per potential: angular pair count (Simp) or nl (Diag) */
     const int* const* pairs; /* per potential: (npairs, 2) int32 (row, col); NULL for Diag */
     const cplx* const* data; /* per potential: (npairs, (2kb+1)*nr) complex128 */
+    int nfuncs;              /* number of distinct time functions (the largest timedep) */
 } orc_operator;
 
 /* PropagatorBase.MultiplyPotential -> TensorPotential.MultiplyPotential for every
  * consolidated potential (Propagator.py:61-66, TensorPotential.py:92-112):
- * dst[row] += s * A_pair * src[col].  s = 1 for static potentials, else `scaling`. */
-void orc_multiply_potentials(const orc_operator* op, double scaling, const cplx* src, cplx* dst) {
+ * dst[row] += s * A_pair * src[col].  s = 1 for static potentials, else the value of the
+ * potential's own time function, scalings[timedep - 1] (each potential is scaled by its
+ * own f(t), TensorPotential.py:98-100). */
+void orc_multiply_potentials(const orc_operator* op, const double* scalings, const cplx* src, cplx* dst) {
     long nr = op->nr;
     int lda = 2 * op->kb + 1;
     for (int p = 0; p < op->npot; p++) {
-        cplx s = { op->timedep[p] ? scaling : 1.0, 0.0 };
+        cplx s = { op->timedep[p] ? scalings[op->timedep[p] - 1] : 1.0, 0.0 };
         const cplx* V = op->data[p];
         if (op->kind[p] == ORC_DIAG_BANDNH) {
 #pragma omp parallel for schedule(static)
@@ -261,13 +264,13 @@ void orc_multiply_potentials(const orc_operator* op, double scaling, const cplx*
 
 /* BasisPropagator.MultiplyHamiltonianBalancedOverlap (BasisPropagator.py:131-159):
  * dst = U^-H  H(t)  U^-1 src, src left unchanged. `work` holds nl*nr entries. */
-void orc_balanced_matvec(const orc_operator* op, double scaling, const cplx* src, cplx* dst, cplx* work) {
+void orc_balanced_matvec(const orc_operator* op, const double* scalings, const cplx* src, cplx* dst, cplx* work) {
     long N = (long)op->nl * op->nr;
     memcpy(work, src, N * sizeof(cplx));                       /* StorePsi + in-place solve */
 #pragma omp parallel for schedule(static)
     for (int l = 0; l < op->nl; l++) ztbsv_upper(op->nr, op->kd, op->U, work + (long)l * op->nr);
     memset(dst, 0, N * sizeof(cplx));                          /* dest = 0 */
-    orc_multiply_potentials(op, scaling, work, dst);
+    orc_multiply_potentials(op, scalings, work, dst);
 #pragma omp parallel for schedule(static)
     for (int l = 0; l < op->nl; l++) ztbsv_upper_conj(op->nr, op->kd, op->U, dst + (long)l * op->nr);
 }
@@ -414,7 +417,7 @@ typedef struct {
 
 /* pAMP::PropagateVector on x (balanced coordinates), one call. V: m*N, H: m*m,
  * r, tmp, work: N each. */
-static int pamp_propagate(const orc_operator* op, double scaling, int m, cplx dt, int double_orth,
+static int pamp_propagate(const orc_operator* op, const double* scalings, int m, cplx dt, int double_orth,
                           cplx* x, cplx* V, cplx* H, cplx* r, cplx* tmp, cplx* work, orc_stats* st) {
     long N = (long)op->nl * op->nr;
     const double tol = sqrt(DBL_EPSILON);          /* pamp.h:79 */
@@ -430,7 +433,7 @@ static int pamp_propagate(const orc_operator* op, double scaling, int m, cplx dt
     memset(V, 0, sizeof(cplx) * m * N);
     memset(H, 0, sizeof(cplx) * m * m);
     memcpy(V, r, N * sizeof(cplx));
-    orc_balanced_matvec(op, scaling, V, r, work); st->operator_count++;
+    orc_balanced_matvec(op, scalings, V, r, work); st->operator_count++;
     cplx alpha = zdotc(N, V, r); st->inner_product_count++;
     zaxpy(N, (cplx){-alpha.re, -alpha.im}, V, r);
     H[0] = alpha;
@@ -445,7 +448,7 @@ static int pamp_propagate(const orc_operator* op, double scaling, int m, cplx dt
         cplx* vj1 = V + (long)(j + 1) * N;
         memcpy(vj1, r, N * sizeof(cplx));
         H[(j + 1) * m + j].re = beta;                              /* H(j+1, j) = beta */
-        orc_balanced_matvec(op, scaling, vj1, r, work); st->operator_count++;
+        orc_balanced_matvec(op, scalings, vj1, r, work); st->operator_count++;
         nbasis = j + 2;
         double orig = global_norm(N, r);
         block_inner(N, j + 2, V, r, ov);
@@ -489,8 +492,8 @@ static int pamp_propagate(const orc_operator* op, double scaling, int m, cplx dt
 }
 
 /* Advance `nsteps` PamPropagator steps (PamPropagator.py:50-57, Problem.py:158-173)
- * on psi (nl*nr complex128, C order psi[l][r]).  scalings[n] is the time function
- * evaluated at the start of step n (TensorPotential.py:98-100 with t=PropagatedTime).
+ * on psi (nl*nr complex128, C order psi[l][r]).  scalings[n * nfuncs + k] is time function
+ * k + 1 evaluated at the start of step n (TensorPotential.py:98-100 with t=PropagatedTime).
  * Returns 0, or the LU info of a failed Pade solve. */
 int orc_advance(const orc_operator* op, cplx* psi, int m, double dt_re, double dt_im,
                 int nsteps, const double* scalings, int double_orth, orc_stats* st) {
@@ -501,10 +504,11 @@ int orc_advance(const orc_operator* op, cplx* psi, int m, double dt_re, double d
     cplx* tmp = (cplx*)malloc(sizeof(cplx) * N);
     cplx* work = (cplx*)malloc(sizeof(cplx) * N);
     cplx dt = { dt_re, dt_im };
+    const int nf = op->nfuncs > 0 ? op->nfuncs : 1;
     int rc = 0;
     for (int n = 0; n < nsteps && !rc; n++) {
         orc_multiply_sqrt_overlap(op, psi);
-        rc = pamp_propagate(op, scalings[n], m, dt, double_orth, psi, V, H, r, tmp, work, st);
+        rc = pamp_propagate(op, scalings + (long)n * nf, m, dt, double_orth, psi, V, H, r, tmp, work, st);
         orc_solve_sqrt_overlap(op, 0, psi);
     }
     free(V); free(H); free(r); free(tmp); free(work);
@@ -513,14 +517,14 @@ int orc_advance(const orc_operator* op, cplx* psi, int m, double dt_re, double d
 
 /* One pAMP call on a vector already in balanced coordinates; exposes H and
  * exp(H) for the small-matrix parity tests. */
-int orc_pamp_once(const orc_operator* op, cplx* x, int m, double dt_re, double dt_im, double scaling,
+int orc_pamp_once(const orc_operator* op, cplx* x, int m, double dt_re, double dt_im, const double* scalings,
                   int double_orth, cplx* H_out, orc_stats* st) {
     long N = (long)op->nl * op->nr;
     cplx* V = (cplx*)malloc(sizeof(cplx) * (long)m * N);
     cplx* r = (cplx*)malloc(sizeof(cplx) * N);
     cplx* tmp = (cplx*)malloc(sizeof(cplx) * N);
     cplx* work = (cplx*)malloc(sizeof(cplx) * N);
-    int rc = pamp_propagate(op, scaling, m, (cplx){dt_re, dt_im}, double_orth, x, V, H_out, r, tmp, work, st);
+    int rc = pamp_propagate(op, scalings, m, (cplx){dt_re, dt_im}, double_orth, x, V, H_out, r, tmp, work, st);
     free(V); free(r); free(tmp); free(work);
     return rc;
 }
@@ -602,7 +606,7 @@ typedef struct {
 } orc_expokit_stats;
 
 /* zgexpv on w (balanced coordinates, in place): w <- exp(t_out * fac * A) w. */
-static int zgexpv(const orc_operator* op, double scaling, int m, double t_out, cplx fac, double tol, double anorm,
+static int zgexpv(const orc_operator* op, const double* scalings, int m, double t_out, cplx fac, double tol, double anorm,
                   cplx* w, cplx* V, cplx* work, orc_expokit_stats* st) {
     long N = (long)op->nl * op->nr;
     int mh = m + 2;
@@ -626,7 +630,7 @@ static int zgexpv(const orc_operator* op, double scaling, int m, double t_out, c
         double avnorm = 0.0;
         for (int j = 0; j < m; j++) {
             cplx* p = V + (long)(j + 1) * N;
-            orc_balanced_matvec(op, scaling, V + (long)j * N, p, work);
+            orc_balanced_matvec(op, scalings, V + (long)j * N, p, work);
             for (long i = 0; i < N; i++) p[i] = cmul(fac, p[i]);
             st->matvecs++;
             for (int i = 0; i <= j; i++) {                   /* modified Gram-Schmidt */
@@ -640,7 +644,7 @@ static int zgexpv(const orc_operator* op, double scaling, int m, double t_out, c
             zscal(N, (cplx){1.0 / hj1j, 0.0}, p);
         }
         if (k1 != 0) {
-            orc_balanced_matvec(op, scaling, V + (long)m * N, work + N, work);
+            orc_balanced_matvec(op, scalings, V + (long)m * N, work + N, work);
             for (long i = 0; i < N; i++) work[N + i] = cmul(fac, work[N + i]);
             st->matvecs++;
             avnorm = global_norm(N, work + N);
@@ -695,9 +699,10 @@ int orc_expokit_advance(const orc_operator* op, cplx* psi, int m, double dt_re, 
     int rc = 0;
     st->substeps = st->rejections = st->matvecs = 0;
     st->error = 0.0; st->hump = 1.0; st->last_step = 0.0;
+    const int nf = op->nfuncs > 0 ? op->nfuncs : 1;
     for (int n = 0; n < nsteps && !rc; n++) {
         orc_multiply_sqrt_overlap(op, psi);
-        rc = zgexpv(op, scalings[n], m, t_out, fac, tol, anorm, psi, V, work, st);
+        rc = zgexpv(op, scalings + (long)n * nf, m, t_out, fac, tol, anorm, psi, V, work, st);
         orc_solve_sqrt_overlap(op, 0, psi);
     }
     free(V); free(work);

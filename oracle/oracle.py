@@ -49,6 +49,7 @@ class OrcOperator(C.Structure):
         ("npairs", C.POINTER(C.c_int)),
         ("pairs", C.POINTER(C.c_void_p)),
         ("data", C.POINTER(C.c_void_p)),
+        ("nfuncs", C.c_int),
     ]
 
 
@@ -73,8 +74,8 @@ def lib():
         L.orc_set_num_threads.argtypes = [C.c_int]
         L.orc_zpbtrf_upper.argtypes = [C.c_int, C.c_int, P]
         L.orc_zpbtrf_upper.restype = C.c_int
-        L.orc_multiply_potentials.argtypes = [C.POINTER(OrcOperator), C.c_double, P, P]
-        L.orc_balanced_matvec.argtypes = [C.POINTER(OrcOperator), C.c_double, P, P, P]
+        L.orc_multiply_potentials.argtypes = [C.POINTER(OrcOperator), P, P, P]
+        L.orc_balanced_matvec.argtypes = [C.POINTER(OrcOperator), P, P, P, P]
         L.orc_multiply_sqrt_overlap.argtypes = [C.POINTER(OrcOperator), P]
         L.orc_solve_sqrt_overlap.argtypes = [C.POINTER(OrcOperator), C.c_int, P]
         L.orc_pade_exponential.argtypes = [C.c_int, P, C.c_int, P]
@@ -84,7 +85,7 @@ def lib():
         L.orc_advance.argtypes = [C.POINTER(OrcOperator), P, C.c_int, C.c_double, C.c_double, C.c_int, P, C.c_int,
                                   C.POINTER(OrcStats)]
         L.orc_advance.restype = C.c_int
-        L.orc_pamp_once.argtypes = [C.POINTER(OrcOperator), P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+        L.orc_pamp_once.argtypes = [C.POINTER(OrcOperator), P, C.c_int, C.c_double, C.c_double, P, C.c_int,
                                     P, C.POINTER(OrcStats)]
         L.orc_pamp_once.restype = C.c_int
         L.orc_expokit_advance.argtypes = [C.POINTER(OrcOperator), P, C.c_int, C.c_double, C.c_double, C.c_int, P,
@@ -148,7 +149,9 @@ class Operator:
 
     U_band:     complex128 (nr*(kd+1),) upper band storage
     potentials: list of dict(kind=ORC_DIAG_BANDNH|ORC_SIMP_BANDNH, data=(npairs, (2kb+1)*nr) complex128,
-                pairs=(npairs, 2) int32 or None, timedep=bool)
+                pairs=(npairs, 2) int32 or None, timedep=False/True or k >= 1: the potential is scaled
+                by time function k (True = 1); nfuncs = the largest k)
+    Scalings: per step either one value (one time function) or nfuncs values.
     """
 
     def __init__(self, nl, nr, kd, kb, U_band, potentials):
@@ -159,15 +162,17 @@ class Operator:
             data = np.ascontiguousarray(p["data"], dtype=np.complex128)
             pairs = p.get("pairs")
             pairs = np.ascontiguousarray(pairs, dtype=np.int32) if pairs is not None else np.zeros((1, 2), np.int32)
-            self.pots.append((int(p["kind"]), int(bool(p["timedep"])), data.shape[0], pairs, data))
+            self.pots.append((int(p["kind"]), int(p["timedep"]), data.shape[0], pairs, data))
         n = len(self.pots)
+        self.nfuncs = max([1] + [q[1] for q in self.pots])
         self._kind = (C.c_int * max(n, 1))(*[q[0] for q in self.pots])
         self._td = (C.c_int * max(n, 1))(*[q[1] for q in self.pots])
         self._np = (C.c_int * max(n, 1))(*[q[2] for q in self.pots])
         self._pairs = (C.c_void_p * max(n, 1))(*[q[3].ctypes.data for q in self.pots])
         self._data = (C.c_void_p * max(n, 1))(*[q[4].ctypes.data for q in self.pots])
         self.op = OrcOperator(nl, nr, kb, kd, self.U.ctypes.data, n, self._kind, self._td, self._np,
-                              C.cast(self._pairs, C.POINTER(C.c_void_p)), C.cast(self._data, C.POINTER(C.c_void_p)))
+                              C.cast(self._pairs, C.POINTER(C.c_void_p)), C.cast(self._data, C.POINTER(C.c_void_p)),
+                              self.nfuncs)
 
     @classmethod
     def from_problem(cls, problem):
@@ -177,17 +182,24 @@ class Operator:
         kd = repr_.radial.kd
         pots = []
         kb = kd
+        nfun = 0
         for p in problem.Propagator.BasePropagator.PotentialList:
             s0, _ = p.GetStorageIds()
             kb = p.GeometryList[1].band_count
+            # every time-dependent consolidated potential is scaled by its own time function
+            # (TensorPotential.py:98-100): number them in list order
+            td = 0
+            if p.IsTimeDependent:
+                nfun += 1
+                td = nfun
             if s0 == "Diag":
-                pots.append(dict(kind=ORC_DIAG_BANDNH, data=p.PotentialData, pairs=None, timedep=p.IsTimeDependent))
+                pots.append(dict(kind=ORC_DIAG_BANDNH, data=p.PotentialData, pairs=None, timedep=td))
             elif s0 == "Simp":
                 pots.append(dict(kind=ORC_SIMP_BANDNH, data=p.PotentialData, pairs=p.GeometryList[0].GetBasisPairs(),
-                                 timedep=p.IsTimeDependent))
+                                 timedep=td))
             elif s0 == "Ident":
                 data = np.repeat(p.PotentialData, nl, axis=0)
-                pots.append(dict(kind=ORC_DIAG_BANDNH, data=data, pairs=None, timedep=p.IsTimeDependent))
+                pots.append(dict(kind=ORC_DIAG_BANDNH, data=data, pairs=None, timedep=td))
             else:
                 raise NotImplementedError(s0)
         return cls(nl, nr, kd, kb, repr_.radial.cholesky_band().astype(np.complex128), pots)
@@ -195,17 +207,32 @@ class Operator:
     def _vec(self, x):
         return np.ascontiguousarray(x, dtype=np.complex128).reshape(self.nl, self.nr).copy()
 
+    def _step_scalings(self, scalings, nsteps=None):
+        """(nsteps, nfuncs) contiguous float64: a value per step for one time function, or
+        nfuncs values per step; a single value is used for every time function."""
+        a = np.asarray(scalings, dtype=np.float64)
+        if nsteps is None:                              # one step
+            a = a.reshape(-1)
+            if a.size == 1:
+                a = np.repeat(a, self.nfuncs)
+            return np.ascontiguousarray(a.reshape(1, self.nfuncs))
+        if a.ndim == 1 and self.nfuncs == 1:
+            a = a.reshape(-1, 1)
+        return np.ascontiguousarray(a.reshape(nsteps, self.nfuncs))
+
     def multiply_potentials(self, src, scaling):
         src = self._vec(src)
         dst = np.zeros_like(src)
-        lib().orc_multiply_potentials(C.byref(self.op), float(scaling), _p(src), _p(dst))
+        s = self._step_scalings(scaling)
+        lib().orc_multiply_potentials(C.byref(self.op), _p(s), _p(src), _p(dst))
         return dst
 
     def balanced_matvec(self, src, scaling):
         src = self._vec(src)
         dst = np.zeros_like(src)
         work = np.zeros_like(src)
-        lib().orc_balanced_matvec(C.byref(self.op), float(scaling), _p(src), _p(dst), _p(work))
+        s = self._step_scalings(scaling)
+        lib().orc_balanced_matvec(C.byref(self.op), _p(s), _p(src), _p(dst), _p(work))
         return dst
 
     def multiply_sqrt_overlap(self, psi):
@@ -221,10 +248,11 @@ class Operator:
     def advance(self, psi, m, dt, scalings, double_orth=False):
         """len(scalings) PamPropagator steps; returns (psi, stats)."""
         x = self._vec(psi)
-        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        n = np.asarray(scalings).shape[0] if np.ndim(scalings) else 1
+        s = self._step_scalings(scalings, n)
         st = OrcStats()
         dt = complex(dt)
-        rc = lib().orc_advance(C.byref(self.op), _p(x), int(m), dt.real, dt.imag, len(s), _p(s),
+        rc = lib().orc_advance(C.byref(self.op), _p(x), int(m), dt.real, dt.imag, n, _p(s),
                                int(bool(double_orth)), C.byref(st))
         if rc:
             raise RuntimeError("oracle Pade LU failed (info %d)" % rc)
@@ -233,10 +261,11 @@ class Operator:
     def expokit_advance(self, psi, m, dt, scalings, tol, anorm):
         """len(scalings) ExpokitPropagator steps (zgexpv, Krylov dimension m); returns (psi, stats)."""
         x = self._vec(psi)
-        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        n = np.asarray(scalings).shape[0] if np.ndim(scalings) else 1
+        s = self._step_scalings(scalings, n)
         st = OrcExpokitStats()
         dt = complex(dt)
-        rc = lib().orc_expokit_advance(C.byref(self.op), _p(x), int(m), dt.real, dt.imag, len(s), _p(s),
+        rc = lib().orc_expokit_advance(C.byref(self.op), _p(x), int(m), dt.real, dt.imag, n, _p(s),
                                        float(tol), float(anorm), C.byref(st))
         if rc:
             raise RuntimeError("oracle Expokit failed (%d)" % rc)
@@ -248,7 +277,8 @@ class Operator:
         H = np.zeros((m, m), dtype=np.complex128)
         st = OrcStats()
         dt = complex(dt)
-        rc = lib().orc_pamp_once(C.byref(self.op), _p(x), int(m), dt.real, dt.imag, float(scaling),
+        s = self._step_scalings(scaling)
+        rc = lib().orc_pamp_once(C.byref(self.op), _p(x), int(m), dt.real, dt.imag, _p(s),
                                  int(bool(double_orth)), _p(H), C.byref(st))
         if rc:
             raise RuntimeError("oracle Pade LU failed (info %d)" % rc)
@@ -260,8 +290,9 @@ class Operator:
         nl, nr, kb = self.nl, self.nr, self.kb
         W = 2 * kb + 1
         H = np.zeros((nl * nr, nl * nr), dtype=np.complex128)
+        sc = self._step_scalings(scaling)[0]
         for kind, td, npairs, pairs, data in self.pots:
-            s = scaling if td else 1.0
+            s = sc[td - 1] if td else 1.0
             for q in range(npairs):
                 row, col = (q, q) if kind == ORC_DIAG_BANDNH else (pairs[q, 0], pairs[q, 1])
                 for i in range(nr):

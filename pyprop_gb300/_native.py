@@ -82,14 +82,17 @@ _PROTOS = {
     "gbprop_advance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_double]),
     "gbprop_advance_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_double]),
     "gbprop_matvec": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
+    "gbprop_matvec_scalings": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "gbprop_multiply_sqrt_overlap": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbprop_set_renormalization": (C.c_int, [C.c_void_p, C.c_int]),
+    "gbprop_inner_product": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gbprop_solve_sqrt_overlap": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "gbprop_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "gbprop_reset_stats": (C.c_int, [C.c_void_p]),
     "gbprop_get_hessenberg": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gbprop_synchronize": (C.c_int, [C.c_void_p]),
     "gbprop_debug_set": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong]),
-    "gbprop_time_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+    "gbprop_time_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                    C.POINTER(StepTimers)]),
     "gbprop_tensor_multiply_bandnh": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double,
                                                 C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
@@ -162,6 +165,7 @@ class Handle:
                               C.c_void_p(stream or 0)))
         self._h = h
         self.nl, self.nr, self.precision, self.m = nl, nr, precision, krylov_basis_size
+        self.nfuncs = 1                 # time functions (the largest number given to add_potential)
 
     def __del__(self):
         try:
@@ -187,26 +191,52 @@ class Handle:
         p = None
         if pairs is not None:
             p = np.ascontiguousarray(pairs, dtype=np.int32)
-        check(lib().gbprop_add_potential(self._h, int(storage), int(npairs), ptr(p), int(kb), ptr(d),
-                                         int(bool(time_dependent))))
+        k = int(time_dependent)        # False/True or a time-function number
+        check(lib().gbprop_add_potential(self._h, int(storage), int(npairs), ptr(p), int(kb), ptr(d), k))
+        self.nfuncs = max(self.nfuncs, k)
 
     def finalize(self):
         check(lib().gbprop_finalize(self._h))
 
-    def advance(self, psi_dev, scalings, dt):
+    def _steps(self, scalings):
+        """(nsteps, K) step-major time-function values: one value per step, or K per step."""
         import numpy as np
-        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        s = np.asarray(scalings, dtype=np.float64)
+        if s.ndim <= 1 and self.nfuncs == 1:
+            s = s.reshape(-1, 1)
+        s = np.ascontiguousarray(s.reshape(-1, self.nfuncs))
+        return s
+
+    def advance(self, psi_dev, scalings, dt):
+        s = self._steps(scalings)
         dt = complex(dt)
-        check(lib().gbprop_advance(self._h, ptr(psi_dev), int(len(s)), ptr(s), dt.real, dt.imag))
+        check(lib().gbprop_advance(self._h, ptr(psi_dev), int(s.shape[0]), ptr(s), dt.real, dt.imag))
 
     def advance_host(self, psi_host, scalings, dt):
-        import numpy as np
-        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        s = self._steps(scalings)
         dt = complex(dt)
-        check(lib().gbprop_advance_host(self._h, ptr(psi_host), int(len(s)), ptr(s), dt.real, dt.imag))
+        check(lib().gbprop_advance_host(self._h, ptr(psi_host), int(s.shape[0]), ptr(s), dt.real, dt.imag))
 
     def matvec(self, src, dst, scaling, balanced=True):
-        check(lib().gbprop_matvec(self._h, ptr(src), ptr(dst), float(scaling), int(bool(balanced))))
+        """dst = (balanced) operator at time-function value(s) `scaling`: one value for every
+        time function, or K values."""
+        import numpy as np
+        v = np.asarray(scaling, dtype=np.float64).reshape(-1)
+        if v.size == 1:
+            check(lib().gbprop_matvec(self._h, ptr(src), ptr(dst), float(v[0]), int(bool(balanced))))
+        else:
+            v = np.ascontiguousarray(v)
+            check(lib().gbprop_matvec_scalings(self._h, ptr(src), ptr(dst), ptr(v), int(bool(balanced))))
+
+    def set_renormalization(self, on):
+        """Every step ends with psi <- psi / ||psi||_S (Problem.py:167-168), on the device."""
+        check(lib().gbprop_set_renormalization(self._h, int(bool(on))))
+
+    def inner_product(self, a, b):
+        """a^H (I x S) b of two device wavefunctions (synchronous)."""
+        out = (C.c_double * 2)()
+        check(lib().gbprop_inner_product(self._h, ptr(a), ptr(b), out))
+        return complex(out[0], out[1])
 
     def multiply_sqrt_overlap(self, psi):
         check(lib().gbprop_multiply_sqrt_overlap(self._h, ptr(psi)))
@@ -237,7 +267,8 @@ class Handle:
         {phase: (ms, launches)}, plus 'total_ms' and 'launches'."""
         dt = complex(dt)
         t = StepTimers()
-        check(lib().gbprop_time_step(self._h, ptr(psi_dev), float(scaling), dt.real, dt.imag, C.byref(t)))
+        s = self._steps(scaling)[:1]
+        check(lib().gbprop_time_step(self._h, ptr(psi_dev), ptr(s), dt.real, dt.imag, C.byref(t)))
         out = {name: (t.ms[k], t.count[k]) for k, name in enumerate(PHASES)}
         out["total_ms"] = t.total_ms
         out["launches"] = t.launches
@@ -249,11 +280,10 @@ class Handle:
 
     def expokit_advance(self, psi_dev, scalings, dt, tol, anorm):
         """Expokit steps (Krylov dimension = this handle's basis size - 1); returns ExpokitStats."""
-        import numpy as np
-        s = np.ascontiguousarray(scalings, dtype=np.float64)
+        s = self._steps(scalings)
         dt = complex(dt)
         st = ExpokitStats()
-        check(lib().gbprop_expokit_advance(self._h, ptr(psi_dev), int(len(s)), ptr(s), dt.real, dt.imag,
+        check(lib().gbprop_expokit_advance(self._h, ptr(psi_dev), int(s.shape[0]), ptr(s), dt.real, dt.imag,
                                            float(tol), float(anorm), C.byref(st)))
         return st
 
@@ -285,13 +315,19 @@ class Batch:
             pass
 
     def advance(self, psis, scalings, dts):
-        """psis: list of device tensors; scalings: (count, nsteps); dts: complex per problem."""
+        """psis: list of device tensors; scalings: per problem a (nsteps,) or (nsteps, K_p)
+        array (a (count, nsteps) array when every problem has one time function); dts: complex
+        per problem."""
         import numpy as np
         P = len(self.handles)
-        s = np.ascontiguousarray(np.asarray(scalings, dtype=np.float64).reshape(P, -1))
+        blocks = [h._steps(scalings[p]) for p, h in enumerate(self.handles)]
+        nsteps = blocks[0].shape[0]
+        if any(b.shape[0] != nsteps for b in blocks):
+            raise ValueError("every problem of a batch advances the same number of steps")
+        s = np.ascontiguousarray(np.concatenate([b.reshape(-1) for b in blocks]))
         d = np.ascontiguousarray(np.array([[complex(x).real, complex(x).imag] for x in dts], dtype=np.float64))
         arr = (C.c_void_p * P)(*[p.data_ptr() for p in psis])
-        check(lib().gbprop_batch_advance(self._b, arr, int(s.shape[1]), ptr(s), ptr(d)))
+        check(lib().gbprop_batch_advance(self._b, arr, int(nsteps), ptr(s), ptr(d)))
 
     def synchronize(self):
         """Wait for the batch; raises GbpropError for a device-side failure of any member."""

@@ -74,6 +74,9 @@ template <typename T> struct DevTables {
 
 struct gbprop_ctx {
     int nl = 0, nr = 0, prec = 0, m = 0, expm_method = 0, double_orth = 0;
+    int nfuncs = 1;                   // distinct time functions (values per schedule step)
+    int renormalize = 0;              // psi.Normalize() after every step (renormalization = True)
+    double2* d_ip = nullptr;          // 2 N complex128: U a, U b of gbprop_inner_product
     long N = 0;
     cudaStream_t stream = nullptr;    // owned capture/work stream (non-blocking)
     cudaStream_t ustream = nullptr;   // caller's stream; ordered against `stream` by events
@@ -515,6 +518,22 @@ void tick(gbprop_ctx* h, int phase) {
     h->timing->push_back({phase, h->tick_pool[k]});
 }
 
+// Every time function at the same value (static operators, the autotuner's timing launches).
+Scalings uniform_scalings(double v) {
+    Scalings sc;
+    for (int k = 0; k < kMaxTimeFuncs; ++k) sc.s[k] = v;
+    return sc;
+}
+
+// Schedule entry of one step from `nf` time-function values.
+SchedEntry sched_entry(const double* vals, int nf, double dt_re, double dt_im) {
+    SchedEntry e;
+    for (int k = 0; k < kMaxTimeFuncs; ++k) e.scaling.s[k] = k < nf ? vals[k] : 0.0;
+    e.dt_re = dt_re;
+    e.dt_im = dt_im;
+    return e;
+}
+
 // Chunking of the inverse solve.  `wide` spreads one problem's rows over the GPU: the
 // chunk count minimises (waves of CTAs) x (FP64 residual elements of one CTA, halo
 // included), the refinement being FP64-issue-bound; otherwise (batches, where other
@@ -655,7 +674,7 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
             GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1, nullptr, bpart));
         tick(h, GBPROP_PHASE_SOLVE);
         // y = sum_t c_t s_t A_t s
-        GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, h->d_sched, h->d_ctrl, 0.0, 1, s));
+        GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, h->d_sched, h->d_ctrl, uniform_scalings(0.0), 1, s));
         tick(h, GBPROP_PHASE_BAND);
         // w = U^-T y
         GB_LAUNCH(ksolve(h, 1, h->d_y, kp, h->d_r, kp, nullptr, kp, 0, 1));
@@ -699,6 +718,11 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
     // x <- beta0 V exp(-i dt H) e1
     GB_LAUNCH(launch_combine(kp, V, h->d_v0, N, h->d_ctrl, h->d_x, s));
     tick(h, GBPROP_PHASE_COMBINE);
+    if (h->renormalize) {
+        // Problem.AdvanceStep: psi.Normalize() when renormalization is on (Problem.py:167-168)
+        GB_LAUNCH(launch_renormalize(h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
+        tick(h, GBPROP_PHASE_OTHER);
+    }
     GB_LAUNCH(launch_step_end(h->d_ctrl, s));
     tick(h, GBPROP_PHASE_OTHER);
     return GBPROP_OK;
@@ -760,11 +784,12 @@ gbprop_status arm_flags(gbprop_ctx* h) {
 gbprop_status report_flags(gbprop_ctx* h, int lu, int nonfinite, int timeout) {
     if (!lu && !nonfinite && !timeout) return GBPROP_OK;
     GB_CUDA(cudaMemsetAsync(&h->d_ctrl->lu_info, 0, 3 * sizeof(int), h->stream));
-    // the first cause: a wait that gave up leaves stale data, a non-finite vector makes the
-    // Pade denominator non-finite too
+    // the first cause: a wait that gave up leaves stale data behind it; a failed Pade solve
+    // leaves the step's exponential undefined, so later norms turn non-finite (the kernels
+    // record no LU failure for a Hessenberg matrix that was non-finite already)
     if (timeout) return fail(GBPROP_ETIMEOUT, "a bounded device-side wait gave up (bulk-copy staging or grid barrier)");
-    if (nonfinite) return fail(GBPROP_ENONFINITE, "non-finite Krylov norm or Hessenberg matrix");
-    return fail(GBPROP_ELU, "Pade denominator singular (LU info " + std::to_string(lu) + ")");
+    if (lu) return fail(GBPROP_ELU, "Pade denominator singular (LU info " + std::to_string(lu) + ")");
+    return fail(GBPROP_ENONFINITE, "non-finite Krylov norm or Hessenberg matrix");
 }
 
 gbprop_status device_errors(gbprop_ctx* h, bool block) {
@@ -860,6 +885,9 @@ gbprop_status gbprop_add_potential(gbprop_handle h, int storage, int npairs, con
     if (kb < 1 || kb > kMaxKd) return fail(GBPROP_EUNSUPPORTED, "radial band half-width must be in [1, 8]");
     if (h->kb >= 0 && kb != h->kb) return fail(GBPROP_EUNSUPPORTED, "all potentials must share one radial band width");
     if (!data) return fail(GBPROP_EINVAL, "null potential data");
+    if (time_dependent < 0 || time_dependent > kMaxTimeFuncs)
+        return fail(GBPROP_EUNSUPPORTED, "time_dependent must be 0 (static) or a time function number 1.." +
+                                         std::to_string(kMaxTimeFuncs));
     if (storage == GBPROP_STORAGE_DIAG && npairs != h->nl) return fail(GBPROP_EINVAL, "Diag storage needs npairs == nl");
     if (storage == GBPROP_STORAGE_IDENT && npairs != 1) return fail(GBPROP_EINVAL, "Ident storage needs npairs == 1");
     if (storage == GBPROP_STORAGE_SIMP) {
@@ -874,7 +902,8 @@ gbprop_status gbprop_add_potential(gbprop_handle h, int storage, int npairs, con
     if (storage == GBPROP_STORAGE_SIMP) p.pairs.assign(pairs, pairs + 2 * (size_t)npairs);
     p.kb = kb;
     p.data.assign(data, data + (size_t)npairs * (2 * kb + 1) * h->nr * 2);
-    p.timedep = time_dependent ? 1 : 0;
+    p.timedep = time_dependent;
+    h->nfuncs = std::max(h->nfuncs, time_dependent);
     h->kb = kb;
     h->pots.push_back(std::move(p));
     return GBPROP_OK;
@@ -998,7 +1027,7 @@ gbprop_status gbprop_advance(gbprop_handle h, void* psi, int nsteps, const doubl
         const int chunk = std::min(nsteps - done, std::max(h->sched_cap, 1024));
         if ((st = ensure_sched(h, chunk))) return st;
         std::vector<SchedEntry> sched(chunk);
-        for (int k = 0; k < chunk; ++k) sched[k] = {scalings[done + k], dt_re, dt_im};
+        for (int k = 0; k < chunk; ++k) sched[k] = sched_entry(scalings + (size_t)(done + k) * h->nfuncs, h->nfuncs, dt_re, dt_im);
         // pageable source: staged before the call returns, so `sched` may go out of scope
         GB_CUDA(cudaMemcpyAsync(h->d_sched, sched.data(), chunk * sizeof(SchedEntry), cudaMemcpyHostToDevice, h->stream));
         GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), h->stream));
@@ -1035,7 +1064,16 @@ gbprop_status gbprop_advance_host(gbprop_handle h, void* psi_host, int nsteps, c
 
 gbprop_status gbprop_matvec(gbprop_handle h, const void* src, void* dst, double scaling, int balanced) {
     if (gbprop_status st = check_handle(h, true)) return st;
-    if (!src || !dst) return fail(GBPROP_EINVAL, "null vector");
+    std::vector<double> v(h->nfuncs, scaling);
+    return gbprop_matvec_scalings(h, src, dst, v.data(), balanced);
+}
+
+gbprop_status gbprop_matvec_scalings(gbprop_handle h, const void* src, void* dst, const double* scalings,
+                                     int balanced) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!src || !dst || !scalings) return fail(GBPROP_EINVAL, "null argument");
+    Scalings scaling = uniform_scalings(0.0);
+    for (int k = 0; k < h->nfuncs; ++k) scaling.s[k] = scalings[k];
     if (src == dst) return fail(GBPROP_EINVAL, "src and dst must differ");
     const int kp = h->kprec();
     cudaStream_t s = h->stream;
@@ -1047,6 +1085,34 @@ gbprop_status gbprop_matvec(gbprop_handle h, const void* src, void* dst, double 
     } else {
         GB_LAUNCH(launch_band_apply(kp, kop(h), src, dst, nullptr, h->d_ctrl, scaling, 0, s));
     }
+    GB_CUDA(h->end());
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_set_renormalization(gbprop_handle h, int on) {
+    if (gbprop_status st = check_handle(h, false)) return st;
+    if ((on != 0) != (h->renormalize != 0)) {
+        h->renormalize = on ? 1 : 0;
+        drop_graph(h);
+    }
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_inner_product(gbprop_handle h, const void* a, const void* b, double* out) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!a || !b || !out) return fail(GBPROP_EINVAL, "null argument");
+    if (gbprop_status st = device_errors(h, false)) return st;
+    const long N = h->N;
+    if (!h->d_ip)
+        if (gbprop_status st = h->dalloc(&h->d_ip, (size_t)2 * N * sizeof(double2) + 4 * sizeof(double))) return st;
+    const int kp = h->kprec();
+    double* d_out = reinterpret_cast<double*>(h->d_ip + 2 * N);
+    GB_CUDA(h->begin());
+    GB_LAUNCH(launch_tbmv(0, h->kd, h->d_ud_phys, h->nl, h->nr, a, kp, h->d_ip, 0, h->stream));
+    GB_LAUNCH(launch_tbmv(0, h->kd, h->d_ud_phys, h->nl, h->nr, b, kp, h->d_ip + N, 0, h->stream));
+    GB_LAUNCH(launch_block_inner(0, h->d_ip, N, 1, h->d_ip + N, 0, d_out, h->d_partials, h->d_counter, h->stream));
+    GB_CUDA(cudaMemcpyAsync(out, d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    GB_CUDA(cudaStreamSynchronize(h->stream));
     GB_CUDA(h->end());
     return GBPROP_OK;
 }
@@ -1115,10 +1181,10 @@ gbprop_status gbprop_synchronize(gbprop_handle h) {
     return device_errors(h, true);
 }
 
-gbprop_status gbprop_time_step(gbprop_handle h, void* psi, double scaling, double dt_re, double dt_im,
+gbprop_status gbprop_time_step(gbprop_handle h, void* psi, const double* scalings, double dt_re, double dt_im,
                                gbprop_step_timers* out) {
     if (gbprop_status st = check_handle(h, true)) return st;
-    if (!psi || !out) return fail(GBPROP_EINVAL, "null argument");
+    if (!psi || !out || !scalings) return fail(GBPROP_EINVAL, "null argument");
     if (gbprop_status st = device_errors(h, false)) return st;
     if (h->tick_pool.empty()) {
         h->tick_pool.resize(4 * kMaxBasis * 8 + 64, nullptr);
@@ -1126,7 +1192,7 @@ gbprop_status gbprop_time_step(gbprop_handle h, void* psi, double scaling, doubl
     }
     gbprop_status st;
     if ((st = ensure_sched(h, 1))) return st;
-    SchedEntry se = {scaling, dt_re, dt_im};
+    SchedEntry se = sched_entry(scalings, h->nfuncs, dt_re, dt_im);
     GB_CUDA(h->begin());
     GB_CUDA(cudaMemcpyAsync(h->d_sched, &se, sizeof(se), cudaMemcpyHostToDevice, h->stream));
     GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), h->stream));
@@ -1201,9 +1267,11 @@ gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
     for (int v = 0; v < band_variant_count(); ++v) {
         h->t64.op.variant = v;
         h->t32.op.variant = v;
-        for (int k = 0; k < 3; ++k) GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, nullptr, h->d_ctrl, 1.0, 0, s));
+        for (int k = 0; k < 3; ++k)
+            GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, nullptr, h->d_ctrl, uniform_scalings(1.0), 0, s));
         GB_CUDA(cudaEventRecord(e0, s));
-        for (int k = 0; k < 10; ++k) GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, nullptr, h->d_ctrl, 1.0, 0, s));
+        for (int k = 0; k < 10; ++k)
+            GB_LAUNCH(launch_band_apply(kp, kop(h), h->d_s, h->d_y, nullptr, h->d_ctrl, uniform_scalings(1.0), 0, s));
         GB_CUDA(cudaEventRecord(e1, s));
         GB_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -1408,7 +1476,7 @@ extern "C" gbprop_status gbprop_expokit_advance(gbprop_handle h, void* psi, int 
     Ctrl c;
     double vnorm = -1.0;
     for (int n = 0; n < nsteps; ++n) {
-        SchedEntry se = {scalings[n], dt_re, dt_im};
+        SchedEntry se = sched_entry(scalings + (size_t)n * h->nfuncs, h->nfuncs, dt_re, dt_im);
         GB_CUDA(cudaMemcpyAsync(h->d_sched, &se, sizeof(se), cudaMemcpyHostToDevice, h->stream));
         double t_now = 0.0, t_new = 0.0, xm = 1.0 / m;
         bool first = true;
@@ -1502,8 +1570,11 @@ extern "C" gbprop_status gbprop_expokit_advance(gbprop_handle h, void* psi, int 
             acc.last_step = t_step;
             ++acc.substeps;
         }
+        if (h->renormalize)                              // Problem.py:167-168, after every step
+            GB_LAUNCH(launch_renormalize(h->d_x, h->N, h->d_partials, h->d_counter, h->d_ctrl, h->stream));
     }
     if ((st = enqueue_leave(h, psi, h->stream))) return st;
+    if ((st = arm_flags(h))) return st;
     GB_CUDA(h->end());
     if (stats) *stats = acc;
     return GBPROP_OK;
@@ -1672,6 +1743,9 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
     for (size_t p = 0; p < P; ++p)
         if (!psi[p]) return fail(GBPROP_EINVAL, "null wavefunction in batch");
     if (gbprop_status st = batch_errors(b, false)) return st;
+    // problem p's nsteps x nfuncs block of the packed scalings
+    std::vector<size_t> off(P + 1, 0);
+    for (size_t p = 0; p < P; ++p) off[p + 1] = off[p] + (size_t)nsteps * b->hs[p]->nfuncs;
     GB_CUDA(cudaEventRecord(b->ev_in, b->ustream));
     GB_CUDA(cudaStreamWaitEvent(b->stream, b->ev_in, 0));
     static const int kShape[4] = {1 | 2 | 4, 1 | 2, 2, 2 | 4};
@@ -1698,8 +1772,9 @@ gbprop_status gbprop_batch_advance(gbprop_batch b, void* const* psi, int nsteps,
             if (gbprop_status st = ensure_sched(h, chunk)) return st;
             if (h->sched_cap != old_cap) recapture = true;
             std::vector<SchedEntry> sched(chunk);
+            const double* sp = scalings + off[p] + (size_t)done * h->nfuncs;
             for (int k = 0; k < chunk; ++k)
-                sched[k] = {scalings[p * (size_t)nsteps + done + k], dt[2 * p], dt[2 * p + 1]};
+                sched[k] = sched_entry(sp + (size_t)k * h->nfuncs, h->nfuncs, dt[2 * p], dt[2 * p + 1]);
             GB_CUDA(cudaMemcpyAsync(h->d_sched, sched.data(), chunk * sizeof(SchedEntry), cudaMemcpyHostToDevice,
                                     b->stream));
             GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), b->stream));

@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(256) k_expm_cluster_df(Ctrl* ctrl, double* Hg,
     const float2* Z = reinterpret_cast<const float2*>(X) + m;   // Z(r, k) = Z[r * w2 + k]
     const int info = gi ? gi : (ctrl->inject_lu ? m : 0);       // inject_lu: host-set test hook
     if (info) {
-        if (rank == 0 && tid == 0) ctrl->lu_info = info;
+        if (rank == 0 && tid == 0 && !ctrl->nonfinite) ctrl->lu_info = info;   // non-finite matrix: that is the cause
     } else {
         const int ncol = (m - rank + CL - 1) / CL;           // this CTA's columns c = rank + j*CL
         float4* Xc = T;

@@ -102,7 +102,7 @@ template <typename T> struct BandOp {
     const int* row_ptr;      // nl + 1
     const int* t_src;        // nterms
     const int* t_slot;       // nterms
-    const int* t_timedep;    // nterms
+    const int* t_timedep;    // nterms: 0 static, k >= 1 scaled by time function k
     const double* t_coef;    // 2 * nterms (re, im)
     const T* slots;
     const T* slots_lo;       // FP32 only: slot - (float)slot, the coefficients' rounding remainder
@@ -141,9 +141,18 @@ struct Ctrl {
     double y[2 * kMaxBasis];
 };
 
-// Schedule entry per step: time-function value and complex time step.
+// Up to this many distinct time functions per handle (the consolidated TensorPotentials of
+// one problem, each scaled by its own f(t), TensorPotential.py:98-100).
+constexpr int kMaxTimeFuncs = 4;
+
+// Values of the time functions at one instant: s[k] scales the terms of time function k + 1.
+struct Scalings {
+    double s[kMaxTimeFuncs];
+};
+
+// Schedule entry per step: the time functions at the step start and the complex time step.
 struct SchedEntry {
-    double scaling;
+    Scalings scaling;
     double dt_re;
     double dt_im;
 };
@@ -183,12 +192,16 @@ cudaError_t launch_solve_inv(const InvTab& tab, int nrows, int refine64, const v
                              int out_prec, void* vstore, int v_prec, Ctrl* ctrl, int dir, int scale_mode,
                              int check_broken, cudaStream_t s, float4* v0s = nullptr, const void* bpart = nullptr,
                              int bG = 0);
+// sched (device, may be null): the time functions come from sched[ctrl->step]; else `scaling`.
 cudaError_t launch_band_apply(int arith, const void* op, const void* x, void* y, const SchedEntry* sched,
-                              const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s);
+                              const Ctrl* ctrl, const Scalings& scaling, int check_broken, cudaStream_t s);
 cudaError_t launch_tbmv(int arith, int kd, const void* ud_phys, int nl, int nr, const void* in, int in_prec,
                         void* out, int out_prec, cudaStream_t s);
 cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsigned* counter, Ctrl* ctrl,
                         cudaStream_t s);
+// x <- x / ||x|| (FP64 state): a k_norm launch and a scaling launch.
+cudaError_t launch_renormalize(double2* x, long n, double* partials, unsigned* counter, Ctrl* ctrl,
+                               cudaStream_t s);
 // v0 (complex64 basis only, may be null): FP64 copy of the first basis vector, used in
 // place of V row 0 by the dot, the update and the combination.
 cudaError_t launch_cgs_dot(int prec, const void* V, const double2* v0, long n, int nv, const void* w,

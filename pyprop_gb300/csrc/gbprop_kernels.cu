@@ -163,9 +163,15 @@ __host__ __device__ constexpr int band_per(int v) { return v == 0 ? 2 : v == 1 ?
 // complex64 band.  Per thread this was ~10 FP64 instructions per term, a large share of
 // the complex64 kernel on a GPU whose FP64 pipe retires two thread operations per clock.
 template <typename T>
-__device__ __forceinline__ void band_term_coef(const BandOp<T>& op, int t, double scal, double2* cd, float4* cf) {
+__device__ __forceinline__ void band_term_coef(const BandOp<T>& op, int t, const double* scal, double2* cd,
+                                               float4* cf) {
     double cr = op.t_coef[2 * t], ci = op.t_coef[2 * t + 1];
-    if (op.t_timedep[t]) { cr *= scal; ci *= scal; }
+    const int td = op.t_timedep[t];
+    if (td) {
+        const double sv = scal[td - 1];
+        cr *= sv;
+        ci *= sv;
+    }
     if constexpr (sizeof(T) == sizeof(double)) {
         *cd = make_double2(cr, ci);
     } else {
@@ -181,7 +187,7 @@ __device__ __forceinline__ void band_term_coef(const BandOp<T>& op, int t, doubl
 template <typename T, int KB, int THREADS, int PER>
 __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T>* __restrict__ x,
                                                         cx<T>* __restrict__ y, const SchedEntry* __restrict__ sched,
-                                                        const Ctrl* __restrict__ ctrl, double scal_val,
+                                                        const Ctrl* __restrict__ ctrl, Scalings scal_val,
                                                         int check_broken) {
     using C = cx<T>;
     constexpr int W = 2 * KB + 1;
@@ -205,7 +211,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
             const int g = i0 - KB + j;
             sx[j] = (g >= 0 && g < nr) ? x[sbase + g] : mk<T>(0, 0);
         }
-        if (tid == 0) band_term_coef(op, t, sched ? sched[ctrl->step].scaling : scal_val, &s_cd, &s_cf);
+        if (tid == 0) band_term_coef(op, t, sched ? sched[ctrl->step].scaling.s : scal_val.s, &s_cd, &s_cf);
         __syncthreads();
         const T* A = op.slots + (size_t)op.t_slot[t] * W * nr;
         T Cr, Ci;
@@ -297,7 +303,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
 template <typename T, int KB, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_band_apply_l1(BandOp<T> op, const cx<T>* __restrict__ x,
                                                            cx<T>* __restrict__ y, const SchedEntry* __restrict__ sched,
-                                                           const Ctrl* __restrict__ ctrl, double scal_val,
+                                                           const Ctrl* __restrict__ ctrl, Scalings scal_val,
                                                            int check_broken) {
     using C = cx<T>;
     constexpr int W = 2 * KB + 1;
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply_l1(BandOp<T> op, const c
         const int tn = min(kTerms, t1 - tg);
         if (tg > t0) __syncthreads();
         if ((int)threadIdx.x < tn)
-            band_term_coef(op, tg + threadIdx.x, sched ? sched[ctrl->step].scaling : scal_val, &s_cd[threadIdx.x],
+            band_term_coef(op, tg + threadIdx.x, sched ? sched[ctrl->step].scaling.s : scal_val.s, &s_cd[threadIdx.x],
                            &s_cf[threadIdx.x]);
         __syncthreads();
         if (!active) continue;
@@ -381,7 +387,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply_l1(BandOp<T> op, const c
 
 template <typename T, int KB, int V>
 static void band_apply_v(const BandOp<T>& op, const void* x, void* y, const SchedEntry* sched, const Ctrl* ctrl,
-                         double scaling, int check_broken, cudaStream_t s) {
+                         const Scalings& scaling, int check_broken, cudaStream_t s) {
     if constexpr (V >= 4) {
         constexpr int TH = band_threads(V);
         dim3 grid((op.nr + TH - 1) / TH, op.nl);
@@ -397,7 +403,7 @@ static void band_apply_v(const BandOp<T>& op, const void* x, void* y, const Sche
 
 template <typename T, int KB>
 static void band_apply_kb(const BandOp<T>& op, const void* x, void* y, const SchedEntry* sched, const Ctrl* ctrl,
-                          double scaling, int check_broken, cudaStream_t s) {
+                          const Scalings& scaling, int check_broken, cudaStream_t s) {
     switch (op.variant) {
         case 0: band_apply_v<T, KB, 0>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
         case 2: band_apply_v<T, KB, 2>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
@@ -410,7 +416,7 @@ static void band_apply_kb(const BandOp<T>& op, const void* x, void* y, const Sch
 
 template <typename T>
 static cudaError_t band_apply_dispatch(const BandOp<T>& op, const void* x, void* y, const SchedEntry* sched,
-                                       const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s) {
+                                       const Ctrl* ctrl, const Scalings& scaling, int check_broken, cudaStream_t s) {
     switch (op.kb) {
 #define GB_KB(K) case K: band_apply_kb<T, K>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
         GB_KB(1) GB_KB(2) GB_KB(3) GB_KB(4) GB_KB(5) GB_KB(6) GB_KB(7) GB_KB(8)
@@ -423,7 +429,7 @@ static cudaError_t band_apply_dispatch(const BandOp<T>& op, const void* x, void*
 int band_variant_count() { return kBandVariants; }
 
 cudaError_t launch_band_apply(int arith, const void* opv, const void* x, void* y, const SchedEntry* sched,
-                              const Ctrl* ctrl, double scaling, int check_broken, cudaStream_t s) {
+                              const Ctrl* ctrl, const Scalings& scaling, int check_broken, cudaStream_t s) {
     count_launch();
     if (arith == 0) return band_apply_dispatch(*(const BandOp<double>*)opv, x, y, sched, ctrl, scaling, check_broken, s);
     return band_apply_dispatch(*(const BandOp<float>*)opv, x, y, sched, ctrl, scaling, check_broken, s);
@@ -518,6 +524,30 @@ __global__ void __launch_bounds__(kRedThreads) k_norm(const CI* __restrict__ x, 
             *counter = 0;
         }
     }
+}
+
+// x <- x / ctrl->beta0 (Problem.AdvanceStep's psi.Normalize(), Problem.py:167-168, on the state in
+// balanced coordinates, where the overlap-metric norm is the Euclidean one); beta0 = ||x|| from
+// the k_norm launched just before.
+__global__ void k_renormalize(double2* __restrict__ x, long n, const Ctrl* __restrict__ ctrl) {
+    const double b = ctrl->beta0;
+    if (!(b > 0.0) || !isfinite(b)) return;          // k_norm has flagged it
+    const double ib = 1.0 / b;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double2 v = x[i];
+        v.x *= ib;
+        v.y *= ib;
+        x[i] = v;
+    }
+}
+
+cudaError_t launch_renormalize(double2* x, long n, double* partials, unsigned* counter, Ctrl* ctrl,
+                               cudaStream_t s) {
+    cudaError_t e = launch_norm(0, x, n, partials, counter, ctrl, s);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    k_renormalize<<<grid_reduce_blocks(), 256, 0, s>>>(x, n, ctrl);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsigned* counter, Ctrl* ctrl,
@@ -1096,7 +1126,7 @@ __global__ void __launch_bounds__(256) k_expm(Ctrl* ctrl, double* Hg, int m, con
     }
     if (!info && ctrl->inject_lu) info = m;       // host-set test hook: report a zero last pivot
     if (info) {
-        if (tid == 0) ctrl->lu_info = info;
+        if (tid == 0 && !ctrl->nonfinite) ctrl->lu_info = info;   // a non-finite matrix is the cause
     } else {
         // zgetrs 'N': apply the row interchanges to P, then L y = b, U x = y (column-parallel axpy form)
         for (int k = 0; k < m; ++k) {
@@ -1314,7 +1344,7 @@ __global__ void __launch_bounds__(256) k_expm_cluster(Ctrl* ctrl, double* Hg, in
     const float2* Z = reinterpret_cast<const float2*>(X) + m;   // the inverse: Z(r, k) = Z[r * w2 + k]
     const int info = s_info ? s_info : (ctrl->inject_lu ? m : 0);   // inject_lu: host-set test hook
     if (info) {
-        if (rank == 0 && tid == 0) ctrl->lu_info = info;
+        if (rank == 0 && tid == 0 && !ctrl->nonfinite) ctrl->lu_info = info;   // non-finite matrix: that is the cause
     } else {
         // this CTA's columns c = rank + j*CL of X (FP64, kept in T), residual R in Q's buffer
         const int ncol = (m - rank + CL - 1) / CL;

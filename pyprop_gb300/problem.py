@@ -8,7 +8,7 @@
 
 Advance() submits the steps between two yields as one device call (the field
 values of those steps are evaluated on the host first, at the times the
-per-step loop would use), unless renormalization is active.
+per-step loop would use); renormalization, when active, happens inside it.
 """
 from __future__ import annotations
 
@@ -106,9 +106,10 @@ class Problem:
         return t + self.TimeStep.real
 
     def AdvanceStep(self):
-        """Problem.AdvanceStep (Problem.py:158-173)."""
+        """Problem.AdvanceStep (Problem.py:158-173).  With renormalization on, the Krylov
+        propagators normalise psi inside the device step (the same psi.Normalize())."""
         self.Propagator.AdvanceStep(self.PropagatedTime, self.TimeStep)
-        if self.Propagator.RenormalizeActive:
+        if self.Propagator.RenormalizeActive and not getattr(self.Propagator, "RenormalizesOnDevice", False):
             self.psi.Normalize()
         self.PropagatedTime = self._next_time(self.PropagatedTime)
 
@@ -116,7 +117,8 @@ class Problem:
         """n consecutive AdvanceStep calls submitted as one device call."""
         if n <= 0:
             return
-        if self.Propagator.RenormalizeActive or not hasattr(self.Propagator, "AdvanceSteps"):
+        if not hasattr(self.Propagator, "AdvanceSteps") or (
+                self.Propagator.RenormalizeActive and not getattr(self.Propagator, "RenormalizesOnDevice", False)):
             for _ in range(n):
                 self.AdvanceStep()
             return

@@ -33,6 +33,27 @@ def _require_device(psi):
         raise RuntimeError("the propagation path runs on the GPU only: wavefunction is on %s" % psi.data.device)
 
 
+MAX_TIME_FUNCTIONS = 4
+
+
+def time_function_numbers(potentials):
+    """The time-function number of every consolidated potential: 0 for static ones, and
+    1, 2, ... for the time-dependent ones in list order.  Each consolidated potential keeps its
+    own time function, evaluated with its own config section (TensorPotential.py:98-100, looped
+    by Propagator.py:61-66); consolidation has already merged potentials sharing one."""
+    nums, k = [], 0
+    for p in potentials:
+        if p.IsTimeDependent:
+            k += 1
+            nums.append(k)
+        else:
+            nums.append(0)
+    if k > MAX_TIME_FUNCTIONS:
+        raise NotImplementedError("%d time-dependent TensorPotentials after consolidation; at most %d"
+                                  % (k, MAX_TIME_FUNCTIONS))
+    return nums
+
+
 def build_handle(psi, potentials, precision=_native.FP64, krylov_basis_size=1, exponentiation_method=0,
                  double_orthogonalization=False):
     """Create and finalize a libgbprop handle for the wavefunction's
@@ -40,18 +61,16 @@ def build_handle(psi, potentials, precision=_native.FP64, krylov_basis_size=1, e
     import torch
     repr_ = psi.GetRepresentation()
     nl, nr = repr_.GetFullShape()
-    tdfuncs = {id(p.OriginalTimeFunction) for p in potentials if p.IsTimeDependent}
-    if len(tdfuncs) > 1:
-        raise NotImplementedError("more than one distinct time function among the TensorPotentials")
+    tf = time_function_numbers(potentials)
     stream = torch.cuda.current_stream().cuda_stream if torch.cuda.is_available() else 0
     h = _native.Handle(nl, nr, precision, krylov_basis_size, exponentiation_method, double_orthogonalization, stream)
     h.set_overlap(repr_.radial.kd, repr_.radial.cholesky_band())
-    for p in potentials:
+    for p, k in zip(potentials, tf):
         s0, s1 = p.GetStorageIds()
         if s1 != "BandNH":
             raise NotImplementedError("radial storage %s" % s1)
         pairs = p.GeometryList[0].GetBasisPairs() if s0 == "Simp" else None
-        h.add_potential(_STORAGE[s0], pairs, p.GeometryList[1].band_count, p.PotentialData, p.IsTimeDependent)
+        h.add_potential(_STORAGE[s0], pairs, p.GeometryList[1].band_count, p.PotentialData, k)
     h.finalize()
     return h
 
@@ -110,28 +129,35 @@ class BasisPropagator(PropagatorBase):
             self._handle = build_handle(self.psi, self.PotentialList, prec, 1)
         return self._handle
 
+    def _scalings_at(self, t):
+        """The time functions at t, in time-function-number order (time_function_numbers);
+        [1.0] when no potential is time dependent."""
+        vals = [p.GetScaling(t) for p in self.PotentialList if p.IsTimeDependent]
+        return np.array(vals or [1.0], dtype=np.float64)
+
     def _scaling(self, t):
-        s = 1.0
-        for p in self.PotentialList:
-            if p.IsTimeDependent:
-                s = p.GetScaling(t)
-        return s
+        """The time function at t, for operators with at most one (the reference's single-pulse
+        configurations); see _scalings_at for several."""
+        v = self._scalings_at(t)
+        if len(v) > 1:
+            raise ValueError("%d time functions: use _scalings_at" % len(v))
+        return float(v[0])
 
     def MultiplyHamiltonian(self, srcPsi, destPsi, t, dt):
         """dest = S^-1 H(t) src (BasisPropagator.py:116-124; SolveOverlap = U^-1 U^-T)."""
         _require_device(srcPsi)
         h = self.Handle()
-        h.matvec(srcPsi.data, destPsi.data, self._scaling(t), balanced=False)
+        h.matvec(srcPsi.data, destPsi.data, self._scalings_at(t), balanced=False)
         h.solve_sqrt_overlap(True, destPsi.data)
         h.solve_sqrt_overlap(False, destPsi.data)
 
     def MultiplyHamiltonianNoOverlap(self, srcPsi, destPsi, t, dt):
         _require_device(srcPsi)
-        self.Handle().matvec(srcPsi.data, destPsi.data, self._scaling(t), balanced=False)
+        self.Handle().matvec(srcPsi.data, destPsi.data, self._scalings_at(t), balanced=False)
 
     def MultiplyHamiltonianBalancedOverlap(self, srcPsi, destPsi, t, dt):
         _require_device(srcPsi)
-        self.Handle().matvec(srcPsi.data, destPsi.data, self._scaling(t), balanced=True)
+        self.Handle().matvec(srcPsi.data, destPsi.data, self._scalings_at(t), balanced=True)
 
     def AdvanceStep(self, t, dt):
         raise NotImplementedError("BasisPropagator does not support AdvanceStep. Use it as a base for explicit propagators")
@@ -171,6 +197,8 @@ class _PampCounters:
 class PamPropagator(PropagatorBase):
     """pAMP Krylov propagator around the balanced-overlap TensorPotential matvec."""
 
+    RenormalizesOnDevice = True     # renormalization = True is applied inside every device step
+
     def __init__(self, psi):
         PropagatorBase.__init__(self, psi)
         self.Rank = psi.GetRank()
@@ -207,14 +235,18 @@ class PamPropagator(PropagatorBase):
         _require_device(self.psi)
         self._handle = build_handle(self.psi, self.BasePropagator.PotentialList, self.Precision, self.BasisSize,
                                     self.ExponentiationMethod, self.DoubleOrthogonalization)
+        # renormalization = True: every step ends with psi.Normalize() on the device
+        self._handle.set_renormalization(self.RenormalizeActive)
         if self.Autotune:
             # pick the band kernel's tile shape for this operator
             self.BandVariant = self._handle.autotune()
         self.BasePropagator.AttachHandle(self._handle)
+        self.psi.AttachHandle(self._handle)
         self.TempPsi = self.psi.CopyDeep()
 
     def _scalings(self, times):
-        return np.array([self.BasePropagator._scaling(t) for t in times], dtype=np.float64)
+        """(len(times), K): the K time functions at the start of every step."""
+        return np.array([self.BasePropagator._scalings_at(t) for t in times], dtype=np.float64)
 
     def AdvanceStep(self, t, dt):
         self.AdvanceSteps([t], dt)
@@ -238,6 +270,8 @@ class ExpokitPropagator(PropagatorBase):
     (core/krylov/expokit/expokitpropagator.cpp:18-103).  Keys: krylov_basis_size,
     krylov_tolerance, krylov_norm (an estimate of the operator's norm, used for the first
     sub-step size)."""
+
+    RenormalizesOnDevice = True
 
     def __init__(self, psi):
         PropagatorBase.__init__(self, psi)
@@ -273,9 +307,11 @@ class ExpokitPropagator(PropagatorBase):
         # m + 1 basis vectors: zgexpv's extra operator application A v_{m+1}
         self._handle = build_handle(self.psi, self.BasePropagator.PotentialList, self.Precision,
                                     self.BasisSize + 1, 0, True)
+        self._handle.set_renormalization(self.RenormalizeActive)
         if self.Autotune:
             self._handle.autotune()
         self.BasePropagator.AttachHandle(self._handle)
+        self.psi.AttachHandle(self._handle)
         self.TempPsi = self.psi.CopyDeep()
 
     def AdvanceStep(self, t, dt):
@@ -284,7 +320,7 @@ class ExpokitPropagator(PropagatorBase):
     def AdvanceSteps(self, times, dt):
         if self._handle is None:
             raise RuntimeError("SetupStep must be called before AdvanceStep")
-        scal = np.array([self.BasePropagator._scaling(t) for t in times], dtype=np.float64)
+        scal = np.array([self.BasePropagator._scalings_at(t) for t in times], dtype=np.float64)
         self.Statistics = self._handle.expokit_advance(self.psi.data, scal, dt, self.Tolerance, self.MatrixNorm)
 
     def MultiplyHamiltonian(self, srcPsi, destPsi, t, dt):

@@ -135,6 +135,7 @@ class Wavefunction:
             device = "cuda" if torch.cuda.is_available() else "cpu"
         self.device = torch.device(device)
         self.data = torch.zeros(representation.GetFullShape(), dtype=self.dtype, device=self.device)
+        self._handle = None             # libgbprop handle of this representation (set by SetupStep)
 
     def GetRank(self):
         return 2
@@ -152,10 +153,16 @@ class Wavefunction:
         torch = _torch()
         self.data.copy_(torch.as_tensor(np.asarray(arr)).to(self.data.dtype))
 
+    def AttachHandle(self, handle):
+        """Route InnerProduct / GetNorm / Normalize of device wavefunctions through the handle's
+        kernels (gbprop_inner_product)."""
+        self._handle = handle
+
     def Copy(self):
         w = Wavefunction.__new__(Wavefunction)
         w.repr, w.dtype, w.device = self.repr, self.dtype, self.device
         w.data = self.data.clone()
+        w._handle = getattr(self, "_handle", None)
         return w
 
     CopyDeep = Copy
@@ -178,6 +185,11 @@ class Wavefunction:
         return out
 
     def InnerProduct(self, other):
+        """<self|other> in the overlap metric.  Device wavefunctions with a handle: libgbprop
+        (gbprop_inner_product); otherwise (host set-up, e.g. initial states) in torch."""
+        h = getattr(self, "_handle", None)
+        if h is not None and self.data.is_cuda and other.data.is_cuda and other.data.dtype == self.data.dtype:
+            return h.inner_product(self.data, other.data)
         torch = _torch()
         So = self._apply_overlap(other.data)
         return complex(torch.sum(torch.conj(self.data.to(torch.complex128)) * So).item())

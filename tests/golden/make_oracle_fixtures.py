@@ -15,11 +15,14 @@ large  hydrogen at scale, l=0..63 x 1000 B-splines, m=30, dt=0.005 (the benchmar
                         5 steps the state depends on the summation order at the 10% level, for the
                         reference's algorithm as for any restatement of it.
          gs0            the hydrogen ground state (1s) in this basis, and
-         gs20/200/2000  the states after 20, 200 and 2000 steps from it (the whole pulse), where
-                        the map is smooth (sensitivity ~3e-15 after 20 steps)
+         gs20/200/2000  the states after 20, 200 and 2000 steps from it (the whole pulse), with
+         gs_sens*       the oracle's sensitivity along that run: the map is smooth while the
+                        field is weak (3e-15 after 20 steps); as the pulse moves population into
+                        the stiff modes it amplifies rounding too (2e-10 after 50 steps, 1e-9
+                        after 100)
 batch  the largest problem size of the 256-problem batch, l=0..64 x 1500 B-splines, r_max=400,
-       m=32, dt=0.01 (oracle_batch_large.npz): the same split -- rand1/sens1 from the seeded
-       random start, gs20 from the ground state gs0
+       m=32, dt=0.01, field from t = 100 (oracle_batch_large.npz): rand1/sens1 from the seeded
+       random start; gs1, gs20 and gs_sens1, gs_sens20 from the ground state gs0
 """
 import os
 import sys
@@ -96,9 +99,10 @@ def large():
     states, _, _ = ob.problem_bound_states(prob, lmax_states=0)
     gs0 = states[0].reshape(psi0.shape).astype(np.complex128)
     gs, st_g = _run(op, gs0, m, dt, scal, [20, 200, 2000], "gs", "large, ground-state start")
+    gsens = {"gs_" + k: v for k, v in _sensitivity(op, gs0, m, dt, scal, [20, 200, 2000]).items()}
     np.savez_compressed(os.path.join(HERE, "oracle_large.npz"), psi0=psi0, scalings=scal, m=m, dt=np.array(dt),
                         gs0=gs0, rand_scaling_order=st_r.last_scaling, gs_scaling_order=st_g.last_scaling,
-                        **rand, **sens, **gs)
+                        **rand, **sens, **gs, **gsens)
 
 
 def batch():
@@ -115,9 +119,10 @@ def batch():
     sens = _sensitivity(op, psi0, p.m, p.dt, scal, [1])
     states, _, _ = ob.hydrogen_bound_states(p, lmax_states=0)
     gs0 = states[0].reshape(psi0.shape).astype(np.complex128)
-    gs, st = _run(op, gs0, p.m, p.dt, scal, [nsteps], "gs", "batch-sized, ground-state start")
+    gs, st = _run(op, gs0, p.m, p.dt, scal, [1, nsteps], "gs", "batch-sized, ground-state start")
+    gsens = {"gs_" + k: v for k, v in _sensitivity(op, gs0, p.m, p.dt, scal, [1, nsteps]).items()}
     np.savez_compressed(os.path.join(HERE, "oracle_batch_large.npz"), psi0=psi0, scalings=scal, m=p.m,
-                        dt=np.array(p.dt), gs0=gs0, gs_scaling_order=st.last_scaling, **rand, **sens, **gs)
+                        dt=np.array(p.dt), gs0=gs0, gs_scaling_order=st.last_scaling, **rand, **sens, **gs, **gsens)
 
 
 if __name__ == "__main__":

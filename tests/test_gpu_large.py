@@ -3,23 +3,25 @@
 Benchmarked workload (pyprop_gb300/configs/hydrogen_velocity_large.ini): hydrogen at scale,
 l = 0..63 x 1000 B-splines, pAMP m = 30, dt = 0.005, the whole 2000-step pulse, through the
 C ABI, against the oracle's states (tests/golden/oracle_large.npz, made by
-tests/golden/make_oracle_fixtures.py) on the same coefficients and field values:
+tests/golden/make_oracle_fixtures.py) on the same coefficients and field values.
 
-  * from the hydrogen ground state, where the step is a smooth map: states after 20, 200 and
-    2000 steps, bar 1e-11 relative L2 (FP64);
-  * from the configured seeded random start, whose random B-spline coefficients fill the
-    stiffest modes (||dt H_m|| ~ 2^17): there the unconverged m = 30 Krylov step amplifies any
-    rounding difference ~1e4-fold per step (the oracle's own response to a 1e-16 relative change
-    of the start is stored as sens1, sens2), so after a few steps the state depends on the
-    summation order for the reference's algorithm itself.  The GPU is compared after 1 and 2
-    steps within 30x that sensitivity.
-
+The stiffest modes of this basis (||dt H_m|| up to 2^17) are far beyond what one m = 30 Krylov
+step resolves, and wherever a state has weight in them the step amplifies any rounding
+difference ~1e4-fold per step -- for the reference's algorithm itself: the oracle's own
+response to a seeded 1e-16 relative change of the start is stored beside every state
+(sens*, gs_sens*).  So the bars are:
+  * from the hydrogen ground state while the map is smooth (the first 20 steps, field still
+    weak; oracle sensitivity 3e-15): 1e-11 relative L2 (FP64);
+  * later along that run (200 and 2000 steps, the pulse has filled stiff modes; oracle
+    sensitivity 4e-9 and 1e-6) and from the configured seeded random start (random B-spline
+    coefficients fill the stiff modes at once; sensitivity 6e-12 after one step, 3e-9 after
+    two): within 30x the oracle's own sensitivity at that point.
 The FP32-mixed form is compared with the same FP64 states from the ground state.
 
 Batch-sized problem: l = 0..64 x 1500 B-splines, r_max = 400, m = 32 (the upper end of the
-batch's sizes), 20 steps from its ground state, alone and as a member of a batch (one-CTA
-exponential, fewest solve chunks), plus one step from its random start within 30x the oracle's
-sensitivity (tests/golden/oracle_batch_large.npz)."""
+batch's sizes), field on from t = 100, alone and as a member of a batch (one-CTA exponential,
+fewest solve chunks): one step from its ground state at the 1e-11 bar, 20 steps and one step
+from its random start within 30x the oracle's sensitivity (tests/golden/oracle_batch_large.npz)."""
 import os
 
 import numpy as np
@@ -67,6 +69,12 @@ def gold():
     return np.load(GOLD_LARGE)
 
 
+def _bar(precision, smooth, sens):
+    if precision == "fp64":
+        return FP64_TOL if smooth else SENS_FACTOR * sens
+    return max(MIXED_TOL, SENS_FACTOR * sens)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
 def test_benchmarked_workload_ground_state_vs_oracle(gold, precision):
     import torch
@@ -75,10 +83,12 @@ def test_benchmarked_workload_ground_state_vs_oracle(gold, precision):
     cdt = torch.complex128 if precision == "fp64" else torch.complex64
     got = _run(h, gold["gs0"], gold["scalings"], complex(gold["dt"]), (20, 200, 2000), cdt)
     errs = {c: rel(x, gold["gs%d" % c]) for c, x in got.items()}
-    print(precision, "ground-state start, relative L2 vs oracle after 20/200/2000 steps:", errs)
+    print(precision, "ground-state start, relative L2 vs oracle after 20/200/2000 steps:", errs,
+          "oracle sensitivity:", {c: float(gold["gs_sens%d" % c]) for c in errs})
     assert h.stats().last_scaling_order == int(gold["gs_scaling_order"])
     for c, e in errs.items():
-        assert e < (FP64_TOL if precision == "fp64" else MIXED_TOL), (c, e)
+        bar = _bar(precision, c == 20, float(gold["gs_sens%d" % c]))
+        assert e < bar, (c, e, bar)
 
 
 def test_benchmarked_workload_random_start_vs_oracle(gold):
@@ -109,12 +119,13 @@ def test_batch_sized_problem_vs_oracle(precision):
     p = _batch_problem()
     assert np.array_equal(p.initial_state(), g["psi0"])
     prec = _native.FP64 if precision == "fp64" else _native.FP32_MIXED
-    tol = FP64_TOL if precision == "fp64" else MIXED_TOL
     cdt = torch.complex128 if precision == "fp64" else torch.complex64
     stream = torch.cuda.current_stream().cuda_stream
+    bars = {1: _bar(precision, True, float(g["gs_sens1"])), 20: _bar(precision, False, float(g["gs_sens20"]))}
     # alone (cluster exponential, solves spread over the GPU)
     h = p.handle(prec, stream)
-    e_alone = rel(_run(h, g["gs0"], g["scalings"], p.dt, (20,), cdt)[20], g["gs20"])
+    got = _run(h, g["gs0"], g["scalings"], p.dt, (1, 20), cdt)
+    e_alone = {c: rel(got[c], g["gs%d" % c]) for c in (1, 20)}
     if precision == "fp64":
         e_rand = rel(_run(h, g["psi0"], g["scalings"], p.dt, (1,), cdt)[1], g["rand1"])
         assert e_rand < SENS_FACTOR * float(g["sens1"]), (e_rand, float(g["sens1"]))
@@ -122,11 +133,15 @@ def test_batch_sized_problem_vs_oracle(precision):
     others = [HydrogenProblem(lmax=3, nr=40, rmax=30.0, m=8, seed=s) for s in (5, 6)]
     bp = BatchPropagator([p] + others, precision=prec, autotune=False)
     bp.psi[0].copy_(torch.as_tensor(g["gs0"]).to(cdt))
-    scal = np.zeros((3, len(g["scalings"])))
-    scal[0] = g["scalings"]
-    bp.batch.advance(bp.psi, scal, [p.dt] + [o.dt for o in others])
-    bp.synchronize()
-    e_batch = rel(bp.psi[0].cpu().numpy().astype(np.complex128), g["gs20"])
-    print(precision, "batch-sized problem, 20 steps from the ground state: alone %.3e, in a batch %.3e" %
-          (e_alone, e_batch))
-    assert e_alone < tol and e_batch < tol
+    e_batch, done = {}, 0
+    for c in (1, 20):
+        scal = np.zeros((3, c - done))
+        scal[0] = g["scalings"][done:c]
+        bp.batch.advance(bp.psi, scal, [p.dt] + [o.dt for o in others])
+        bp.synchronize()
+        e_batch[c] = rel(bp.psi[0].cpu().numpy().astype(np.complex128), g["gs%d" % c])
+        done = c
+    print(precision, "batch-sized problem from the ground state: alone", e_alone, "in a batch", e_batch,
+          "bars", bars)
+    for c in (1, 20):
+        assert e_alone[c] < bars[c] and e_batch[c] < bars[c], (c, e_alone[c], e_batch[c], bars[c])
