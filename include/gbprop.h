@@ -74,7 +74,9 @@ long long gbprop_launch_count(void);
  * core/krylov/pamp/pampwrapper.h:15-123) + the TensorPotential list of
  * BasisPropagator (pyprop/tensorpotential/BasisPropagator.py:41-108).
  *   krylov_basis_size       config key krylov_basis_size (pampwrapper.cpp:53)
- *   exponentiation_method   krylov_exponentiation_method (pampwrapper.cpp:56-61); 0 = Pade only
+ *   exponentiation_method   krylov_exponentiation_method (pampwrapper.cpp:56-61): 0 = Pade
+ *                           scaling-and-squaring (pamp.h:430-564), 1 = eigenvector exponential
+ *                           (pamp.h:567-607)
  *   double_orthogonalization krylov_double_orthogonalization (pampwrapper.cpp:64-69)
  * stream: the CUDA stream every call of this handle is ordered on. */
 gbprop_status gbprop_create(gbprop_handle* out, int nl, int nr, int precision,

@@ -415,15 +415,13 @@ typedef struct {
     int last_basis;          /* Krylov vectors built in the last step */
 } orc_stats;
 
-/* pAMP::PropagateVector on x (balanced coordinates), one call. V: m*N, H: m*m,
- * r, tmp, work: N each. */
-static int pamp_propagate(const orc_operator* op, const double* scalings, int m, cplx dt, int double_orth,
-                          cplx* x, cplx* V, cplx* H, cplx* r, cplx* tmp, cplx* work, orc_stats* st) {
+/* The Arnoldi part of pAMP::PropagateVector on x (balanced coordinates): beta0 = ||x||
+ * (returned), the m basis vectors V (m*N) and the Hessenberg matrix H (m*m, H(i, j) =
+ * <v_i, A v_j> at H[i*m + j]).  ov, ov3: m + 1 each; r, tmp, work: N each. */
+static double pamp_arnoldi(const orc_operator* op, const double* scalings, int m, int double_orth, const cplx* x,
+                           cplx* V, cplx* H, cplx* r, cplx* tmp, cplx* work, cplx* ov, cplx* ov3, orc_stats* st) {
     long N = (long)op->nl * op->nr;
     const double tol = sqrt(DBL_EPSILON);          /* pamp.h:79 */
-    cplx* ov = (cplx*)malloc(sizeof(cplx) * (m + 1));
-    cplx* ov3 = (cplx*)malloc(sizeof(cplx) * (m + 1));
-    cplx* E = (cplx*)malloc(sizeof(cplx) * m * m);
 
     memcpy(r, x, N * sizeof(cplx));                               /* Residual = input */
     double norm = global_norm(N, r);                               /* pamp.h:619-620 */
@@ -472,6 +470,19 @@ static int pamp_propagate(const orc_operator* op, const double* scalings, int m,
         for (int k = 0; k < j + 2; k++) H[k * m + (j + 1)] = ov[k];  /* column j+1 */
     }
     (void)breakdown;
+    st->last_basis = nbasis;
+    return norm;
+}
+
+/* pAMP::PropagateVector on x (balanced coordinates), one call. V: m*N, H: m*m,
+ * r, tmp, work: N each. */
+static int pamp_propagate(const orc_operator* op, const double* scalings, int m, cplx dt, int double_orth,
+                          cplx* x, cplx* V, cplx* H, cplx* r, cplx* tmp, cplx* work, orc_stats* st) {
+    long N = (long)op->nl * op->nr;
+    cplx* ov = (cplx*)malloc(sizeof(cplx) * (m + 1));
+    cplx* ov3 = (cplx*)malloc(sizeof(cplx) * (m + 1));
+    cplx* E = (cplx*)malloc(sizeof(cplx) * m * m);
+    const double norm = pamp_arnoldi(op, scalings, m, double_orth, x, V, H, r, tmp, work, ov, ov3, st);
 
     /* HessenbergMatrix *= -dt * i  (pamp.h:634) */
     cplx f = { dt.im, -dt.re };                                    /* -i*dt */
@@ -480,7 +491,6 @@ static int pamp_propagate(const orc_operator* op, const double* scalings, int m,
     int info = orc_scaling_pade_exponential(m, H, 6, E, &s);
     if (info) st->pade_info = info;
     st->last_scaling = s;
-    st->last_basis = nbasis;
 
     /* y = first column of exp(H); x = norm * V^T y  (pamp.h:657-662) */
     for (int k = 0; k < m; k++) ov[k] = E[k * m + 0];
@@ -513,6 +523,22 @@ int orc_advance(const orc_operator* op, cplx* psi, int m, double dt_re, double d
     }
     free(V); free(H); free(r); free(tmp); free(work);
     return rc;
+}
+
+/* The Arnoldi part of one pAMP call on x (balanced coordinates, unchanged): V (m*N), the
+ * unscaled Hessenberg matrix H (m*m), and beta0 = ||x|| in *norm_out.  Used to restate the
+ * eigenvector exponential (pamp.h:567-607), whose zgeev the caller runs. */
+int orc_arnoldi(const orc_operator* op, const cplx* x, int m, const double* scalings, int double_orth,
+                cplx* V_out, cplx* H_out, double* norm_out, orc_stats* st) {
+    long N = (long)op->nl * op->nr;
+    cplx* r = (cplx*)malloc(sizeof(cplx) * N);
+    cplx* tmp = (cplx*)malloc(sizeof(cplx) * N);
+    cplx* work = (cplx*)malloc(sizeof(cplx) * N);
+    cplx* ov = (cplx*)malloc(sizeof(cplx) * (m + 1));
+    cplx* ov3 = (cplx*)malloc(sizeof(cplx) * (m + 1));
+    *norm_out = pamp_arnoldi(op, scalings, m, double_orth, x, V_out, H_out, r, tmp, work, ov, ov3, st);
+    free(r); free(tmp); free(work); free(ov); free(ov3);
+    return 0;
 }
 
 /* One pAMP call on a vector already in balanced coordinates; exposes H and

@@ -91,6 +91,9 @@ def lib():
         L.orc_expokit_advance.argtypes = [C.POINTER(OrcOperator), P, C.c_int, C.c_double, C.c_double, C.c_int, P,
                                           C.c_double, C.c_double, C.POINTER(OrcExpokitStats)]
         L.orc_expokit_advance.restype = C.c_int
+        L.orc_arnoldi.argtypes = [C.POINTER(OrcOperator), P, C.c_int, P, C.c_int, P, P, C.POINTER(C.c_double),
+                                  C.POINTER(OrcStats)]
+        L.orc_arnoldi.restype = C.c_int
         _lib = L
     return _lib
 
@@ -256,6 +259,35 @@ class Operator:
                                int(bool(double_orth)), C.byref(st))
         if rc:
             raise RuntimeError("oracle Pade LU failed (info %d)" % rc)
+        return x, st
+
+    def advance_eigenvector(self, psi, m, dt, scalings, double_orth=False):
+        """len(scalings) PamPropagator steps with krylov_exponentiation_method = 1
+        (pAMP::EigenvectorExponential, core/krylov/pamp/pamp/pamp.h:567-607): the Arnoldi part in C
+        (orc_arnoldi, the same as every step), then A = -i dt H_m, zgeev (numpy.linalg.eig calls
+        LAPACK zgeev, the routine the reference calls) for eigenvalues lam and unit right
+        eigenvectors W, exp(A) ~ W diag(e^lam) W^H (the reference's formula: W^H, exact for a
+        normal A), y = its first column, x = beta0 V^T y (pamp.h:657-662).  Returns (psi, stats)."""
+        x = self._vec(psi)
+        n = np.asarray(scalings).shape[0] if np.ndim(scalings) else 1
+        s = self._step_scalings(scalings, n)
+        dt = complex(dt)
+        st = OrcStats()
+        N = self.nl * self.nr
+        V = np.zeros((m, N), dtype=np.complex128)
+        H = np.zeros((m, m), dtype=np.complex128)
+        for k in range(n):
+            lib().orc_multiply_sqrt_overlap(C.byref(self.op), _p(x))
+            norm = C.c_double()
+            sk = np.ascontiguousarray(s[k])
+            lib().orc_arnoldi(C.byref(self.op), _p(x), int(m), _p(sk), int(bool(double_orth)), _p(V), _p(H),
+                              C.byref(norm), C.byref(st))
+            A = -1j * dt * H
+            lam, W = np.linalg.eig(A)
+            y = (W * np.exp(lam)[None, :]) @ W[0].conj()
+            x = np.ascontiguousarray((norm.value * (y @ V)).reshape(self.nl, self.nr))
+            lib().orc_solve_sqrt_overlap(C.byref(self.op), 0, _p(x))
+            st.error_estimate = abs(y[m - 1]) ** 2
         return x, st
 
     def expokit_advance(self, psi, m, dt, scalings, tol, anorm):

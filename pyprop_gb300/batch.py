@@ -144,6 +144,49 @@ def random_batch(count=256, seed=20261204, lmax=(8, 64), nr=(200, 1500), rmax=(1
     return probs
 
 
+def step_bytes(problem, elem=16):
+    """Algorithmic bytes of one Krylov step of a problem: s * N * (m^2 + 7m + 3) (the fused
+    step's minimum: the m matvecs' vectors, the Gram-Schmidt passes over the basis, the final
+    combination)."""
+    return elem * problem.N * (problem.m * problem.m + 7 * problem.m + 3)
+
+
+def shard(problems, world, elem=16):
+    """Split one batch over `world` GPUs with no communication during propagation: greedy
+    bin-packing by the per-step work (largest first onto the least-loaded rank, ties to the lower
+    rank).  Returns one sorted list of problem indices per rank; every problem is on exactly one
+    rank.  Deterministic, so every rank computes the same plan without exchanging it."""
+    order = sorted(range(len(problems)), key=lambda i: (-step_bytes(problems[i], elem), i))
+    load = [0] * world
+    out = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(i)
+        load[r] += step_bytes(problems[i], elem)
+    return [sorted(x) for x in out]
+
+
+def gather_states(states, indices, world, count):
+    """All ranks' final states back in batch order on rank 0 (host numpy arrays; a list of
+    `count` arrays on rank 0, None elsewhere).  `indices` are this rank's problems (shard())."""
+    if world == 1:
+        out = [None] * count
+        for i, x in zip(indices, states):
+            out[i] = x
+        return out
+    import torch.distributed as dist
+    mine = list(zip(indices, states))
+    allp = [None] * world if dist.get_rank() == 0 else None
+    dist.gather_object(mine, allp, dst=0)
+    if dist.get_rank() != 0:
+        return None
+    out = [None] * count
+    for part in allp:
+        for i, x in part:
+            out[i] = x
+    return out
+
+
 class BatchPropagator:
     """Advances a list of HydrogenProblem together: one batch step = one
     PamPropagator step of every problem (each with its own field and dt)."""

@@ -713,7 +713,10 @@ gbprop_status enqueue_step(gbprop_ctx* h) {
     const long N = h->N;
     char* V = (char*)h->d_V;
     if (gbprop_status st = enqueue_arnoldi(h, h->double_orth, std::sqrt(DBL_EPSILON))) return st;   // pamp.h:79
-    GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s, h->prec != GBPROP_FP64));
+    if (h->expm_method == 1)                               // EigenvectorExponential (pamp.h:567-607)
+        GB_LAUNCH(launch_expm_eig(h->d_ctrl, h->d_H, m, h->d_sched, s));
+    else                                                   // ScalingPadeExponential (pamp.h:430-564)
+        GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s, h->prec != GBPROP_FP64));
     tick(h, GBPROP_PHASE_EXPONENTIAL);
     // x <- beta0 V exp(-i dt H) e1
     GB_LAUNCH(launch_combine(kp, V, h->d_v0, N, h->d_ctrl, h->d_x, s));
@@ -832,8 +835,8 @@ gbprop_status gbprop_create(gbprop_handle* out, int nl, int nr, int precision, i
     if (precision != GBPROP_FP64 && precision != GBPROP_FP32_MIXED) return fail(GBPROP_EINVAL, "unknown precision");
     if (krylov_basis_size < 1 || krylov_basis_size > kMaxBasis)
         return fail(GBPROP_EINVAL, "krylov_basis_size must be in [1, 45]");
-    if (exponentiation_method != 0)
-        return fail(GBPROP_EUNSUPPORTED, "krylov_exponentiation_method=1 (eigenvector) is not provided; use 0 (Pade)");
+    if (exponentiation_method != 0 && exponentiation_method != 1)
+        return fail(GBPROP_EINVAL, "krylov_exponentiation_method must be 0 (Pade) or 1 (eigenvector)");
     gbprop_ctx* h = new gbprop_ctx();
     h->nl = nl;
     h->nr = nr;

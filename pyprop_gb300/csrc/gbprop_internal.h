@@ -235,6 +235,8 @@ cudaError_t launch_step_begin(Ctrl* ctrl, double* H, int m, cudaStream_t s);
 // df32 = 1 (FP32-mixed handles): the cluster form in double-float arithmetic (gbprop_expm.cu).
 cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s,
                         int df32 = 0);
+// krylov_exponentiation_method = 1 (pamp.h:567-607): y from the eigen-decomposition, one CTA.
+cudaError_t launch_expm_eig(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s);
 // cluster: 16 or 8 CTAs, or 1 (one CTA, for batches; when expm_df_single_fits(m))
 cudaError_t launch_expm_df(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int cluster, cudaStream_t s);
 bool expm_df_single_fits(int m);

@@ -994,6 +994,8 @@ __device__ void smem_matmul(int m, const double2* A, const double2* B, double2* 
 }
 
 __device__ __forceinline__ double cabs1d(double2 a) { return fabs(a.x) + fabs(a.y); }
+__device__ __forceinline__ double2 cadd2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 conjz(double2 a) { return make_double2(a.x, -a.y); }
 
 __device__ double2 cdivz(double2 a, double2 b) {
     // Smith's algorithm
@@ -1492,6 +1494,156 @@ int expm_cluster_size(int m) {
         else g_expm_cluster[m] = 1;
     }
     return g_expm_cluster[m] == 1 ? 0 : g_expm_cluster[m];
+}
+
+// ---------------------------------------------------------------------------
+// pAMP::EigenvectorExponential (pamp.h:567-607; krylov_exponentiation_method = 1,
+// pampwrapper.cpp:56-61): y = exp(A) e1 for A = -i dt H_m from the eigen-decomposition of A.
+// The reference takes zgeev's unit right eigenvectors W and forms W diag(e^lambda) W^H, which is
+// exp(A) for a normal A; for Arnoldi on the Hermitian balanced operator H_m is Hermitian (to
+// rounding) and A normal, so the same y is formed from the eigen-decomposition of the Hermitian
+// part of H_m, H_m = Q diag(mu) Q^H, lambda = -i dt mu:  y = Q (e^{-i dt mu} .* conj(Q(0, :))).
+// The decomposition is a parallel cyclic Jacobi iteration on one CTA (round-robin pairing of
+// the m (padded to even) indices, m/2 disjoint complex rotations per round, applied to the
+// columns and then to the rows), FP64, until the off-diagonal part is below 1e-15 of the matrix
+// (Frobenius) or after 20 sweeps.  Writes -i dt H_m back (GetHessenbergMatrix), y, |y[m-1]|^2.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_expm_eig(Ctrl* ctrl, double* Hg, int m, const SchedEntry* sched) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int mp = m + (m & 1);
+    double2* A = reinterpret_cast<double2*>(smem_raw);     // mp x mp
+    double2* Q = A + mp * mp;                               // mp x mp
+    constexpr int kPairs = (kMaxBasis + 1) / 2;
+    __shared__ int s_p[kPairs], s_q[kPairs];
+    __shared__ double2 s_g[kPairs][4];                      // (g_pp, g_pq, g_qp, g_qq) of pair k
+    __shared__ double s_off[8], s_tot[8];
+    __shared__ int s_go;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const SchedEntry se = sched[ctrl->step];
+    const double2 f = make_double2(se.dt_im, -se.dt_re);   // -i dt
+    for (int k = tid; k < mp * mp; k += blockDim.x) {
+        const int i = k / mp, j = k - i * mp;
+        double2 a = make_double2(0.0, 0.0);
+        if (i < m && j < m) {
+            const double2 hij = make_double2(Hg[2 * (i * m + j)], Hg[2 * (i * m + j) + 1]);
+            const double2 hji = make_double2(Hg[2 * (j * m + i)], Hg[2 * (j * m + i) + 1]);
+            a = make_double2(0.5 * (hij.x + hji.x), 0.5 * (hij.y - hji.y));   // Hermitian part
+        }
+        A[k] = a;
+        Q[k] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    }
+    __syncthreads();
+    // -i dt H_m kept in global, as the Pade kernels do (read back by GetHessenbergMatrix)
+    for (int k = tid; k < m * m; k += blockDim.x) {
+        const double2 h = make_double2(Hg[2 * k], Hg[2 * k + 1]);
+        const double2 a = cmulz(h, f);
+        Hg[2 * k] = a.x;
+        Hg[2 * k + 1] = a.y;
+    }
+    const int npairs = mp / 2;
+    for (int sweep = 0; sweep < 20; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int k = tid; k < mp * mp; k += blockDim.x) {
+            const double2 a = A[k];
+            const double v = a.x * a.x + a.y * a.y;
+            tot += v;
+            if (k / mp != k % mp) off += v;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            off += __shfl_xor_sync(0xffffffffu, off, o);
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        }
+        if (lane == 0) { s_off[warp] = off; s_tot[warp] = tot; }
+        __syncthreads();
+        if (tid == 0) {
+            double o2 = 0.0, t2 = 0.0;
+            for (int w = 0; w < nw; ++w) { o2 += s_off[w]; t2 += s_tot[w]; }
+            s_go = o2 > 1e-30 * t2;
+        }
+        __syncthreads();
+        if (!s_go) break;
+        for (int r = 0; r < mp - 1; ++r) {
+            if (tid < npairs) {
+                auto idx = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + r) % (mp - 1); };
+                int p = idx(tid), q = idx(mp - 1 - tid);
+                if (p > q) { const int t = p; p = q; q = t; }
+                double2 g0 = make_double2(1.0, 0.0), g1 = make_double2(0.0, 0.0), g2 = g1, g3 = g0;
+                const double2 c = A[p * mp + q];
+                const double rr = hypot(c.x, c.y);
+                if (q < m && rr > 0.0) {
+                    const double a = A[p * mp + p].x, b = A[q * mp + q].x;
+                    const double tau = (b - a) / (2.0 * rr);
+                    const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                    const double cs = 1.0 / sqrt(1.0 + t * t), sn = t * cs;
+                    const double er = c.x / rr, ei = -c.y / rr;    // e^{-i phi}
+                    g0 = make_double2(cs, 0.0);
+                    g1 = make_double2(sn, 0.0);
+                    g2 = make_double2(-sn * er, -sn * ei);
+                    g3 = make_double2(cs * er, cs * ei);
+                }
+                s_p[tid] = p;
+                s_q[tid] = q;
+                s_g[tid][0] = g0; s_g[tid][1] = g1; s_g[tid][2] = g2; s_g[tid][3] = g3;
+            }
+            __syncthreads();
+            // A <- A G and Q <- Q G (columns p, q of every pair)
+            for (int k = tid; k < npairs * mp; k += blockDim.x) {
+                const int pr = k / mp, i = k - pr * mp;
+                const int p = s_p[pr], q = s_q[pr];
+                const double2 gpp = s_g[pr][0], gpq = s_g[pr][1], gqp = s_g[pr][2], gqq = s_g[pr][3];
+                double2 ap = A[i * mp + p], aq = A[i * mp + q];
+                A[i * mp + p] = cadd2(cmulz(ap, gpp), cmulz(aq, gqp));
+                A[i * mp + q] = cadd2(cmulz(ap, gpq), cmulz(aq, gqq));
+                ap = Q[i * mp + p];
+                aq = Q[i * mp + q];
+                Q[i * mp + p] = cadd2(cmulz(ap, gpp), cmulz(aq, gqp));
+                Q[i * mp + q] = cadd2(cmulz(ap, gpq), cmulz(aq, gqq));
+            }
+            __syncthreads();
+            // A <- G^H A (rows p, q of every pair)
+            for (int k = tid; k < npairs * mp; k += blockDim.x) {
+                const int pr = k / mp, j = k - pr * mp;
+                const int p = s_p[pr], q = s_q[pr];
+                const double2 gpp = conjz(s_g[pr][0]), gpq = conjz(s_g[pr][1]), gqp = conjz(s_g[pr][2]),
+                              gqq = conjz(s_g[pr][3]);
+                const double2 ap = A[p * mp + j], aq = A[q * mp + j];
+                A[p * mp + j] = cadd2(cmulz(gpp, ap), cmulz(gqp, aq));
+                A[q * mp + j] = cadd2(cmulz(gpq, ap), cmulz(gqq, aq));
+            }
+            __syncthreads();
+        }
+    }
+    // y_k = sum_j Q(k, j) e^{-i dt mu_j} conj(Q(0, j))
+    for (int k = tid; k < m; k += blockDim.x) {
+        double yr = 0.0, yi = 0.0;
+        for (int j = 0; j < m; ++j) {
+            const double mu = A[j * mp + j].x;
+            double sn, cs;
+            sincos(se.dt_re * mu, &sn, &cs);
+            const double amp = exp(se.dt_im * mu);
+            const double2 e = make_double2(amp * cs, -amp * sn);
+            const double2 w = cmulz(Q[k * mp + j], conjz(Q[j]));
+            const double2 t = cmulz(w, e);
+            yr += t.x;
+            yi += t.y;
+        }
+        ctrl->y[2 * k] = yr;
+        ctrl->y[2 * k + 1] = yi;
+        if (k == m - 1) ctrl->err_est = yr * yr + yi * yi;
+    }
+    if (tid == 0) ctrl->scaling_order = 0;
+}
+
+cudaError_t launch_expm_eig(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, cudaStream_t s) {
+    count_launch();
+    const int mp = m + (m & 1);
+    const size_t smem = (size_t)2 * mp * mp * sizeof(double2);
+    if (smem > 48 * 1024) {
+        cudaError_t e = allow_max_smem(k_expm_eig);
+        if (e != cudaSuccess) return e;
+    }
+    k_expm_eig<<<1, 256, smem, s>>>(ctrl, H, m, sched);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_expm(Ctrl* ctrl, double* H, int m, const SchedEntry* sched, int max_cluster, cudaStream_t s,

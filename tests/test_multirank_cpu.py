@@ -1,7 +1,8 @@
 """The N > 1 host logic of bench.py on two CPU ranks over gloo: one rendezvous on 127.0.0.1,
 the max-over-ranks timing every rank agrees on, the barrier, each rank's own shard of independent
-batch problems (no data-path collective), and the reference arm running on rank 0 only.  The
-single-problem step does not shard (replicas); the batch does (weak scaling)."""
+batch problems of one seeded batch, bin-packed by per-step work (no data-path collective; the
+final states are gathered on rank 0), and the reference arm running on rank 0 only.  The
+single-problem step does not shard (replicas); the batch does."""
 import io
 import os
 import socket
@@ -32,8 +33,19 @@ def _worker(rank, world, port, q):
         r, w, _ = bench._dist()
         t = bench._max_over_ranks(1.5 * (r + 1), w)          # per-rank "elapsed" seconds
         bench._barrier(w)
-        from pyprop_gb300.batch import random_batch
-        shard = [(p.lmax, p.nr, p.m, round(p.rmax, 6)) for p in random_batch(4, seed=20261204 + r)]
+        import numpy as np
+        from pyprop_gb300.batch import gather_states, random_batch, shard as shard_of, step_bytes
+        # one seeded batch, this rank's bin-packed share of it, a per-problem result gathered on rank 0
+        full = random_batch(12, seed=20261204, lmax=(2, 9), nr=(30, 90), rmax=(20.0, 60.0))
+        plan = shard_of(full, w)
+        mine = plan[r]
+        states = [full[i].initial_state() for i in mine]
+        got = gather_states(states, mine, w, len(full))
+        ok = None
+        if r == 0:
+            ok = all(np.array_equal(got[i], full[i].initial_state()) for i in range(len(full)))
+        loads = [sum(step_bytes(full[i]) for i in part) for part in plan]
+        shard = (mine, plan, loads, ok)
         # the reference arm: rank 0 does the work, every other rank returns at once, silent
         out = io.StringIO()
         if r != 0:
@@ -61,7 +73,11 @@ def test_two_rank_timing_barrier_and_batch_shards():
     for r, w, t, shard, out in res:
         assert w == 2, t
     assert [x[2] for x in res] == [3.0, 3.0]              # max over ranks, seen by both
-    assert res[0][3] != res[1][3]                          # each rank its own shard of problems
+    (mine0, plan0, loads, ok), (mine1, plan1, _, ok1) = res[0][3], res[1][3]
+    assert plan0 == plan1                                  # every rank computes the same plan
+    assert sorted(mine0 + mine1) == list(range(12)) and not set(mine0) & set(mine1)   # disjoint, complete
+    assert max(loads) <= 1.05 * (sum(loads) / 2)           # per-step work balanced within 5%
+    assert ok is True and ok1 is None                      # rank 0 holds every problem's state
     assert res[1][4] == ""                                 # no reference work or output on rank 1
     assert all(p.exitcode == 0 for p in procs)
 

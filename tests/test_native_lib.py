@@ -31,8 +31,8 @@ def test_version_and_errors_without_device():
     assert st == 1 and b"positive" in L.gbprop_last_error()
     st = L.gbprop_create(ctypes.byref(h), 4, 10, 0, 99, 0, 0, None)
     assert st == 1 and b"krylov_basis_size" in L.gbprop_last_error()
-    st = L.gbprop_create(ctypes.byref(h), 4, 10, 0, 20, 1, 0, None)
-    assert st == 7
+    st = L.gbprop_create(ctypes.byref(h), 4, 10, 0, 20, 2, 0, None)   # exponentiation methods are 0 and 1
+    assert st == 1 and b"krylov_exponentiation_method" in L.gbprop_last_error()
     st = L.gbprop_tensor_multiply_bandnh(5, None, 0, None, 1, 1.0, None, None, 1, 1, None)
     assert st == 7
     st = L.gbprop_advance(None, None, 1, None, 0.1, 0.0)
