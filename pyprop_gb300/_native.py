@@ -334,5 +334,22 @@ class Batch:
         check(lib().gbprop_batch_synchronize(self._b))
 
 
+def block_inner_product(V, w, want_norm=False, stream=None):
+    """conj(V) @ w for the rows of a device matrix V (nv <= 45 rows of n elements, complex128 or
+    complex64, like w) through gbprop_block_inner_product; with want_norm, ||w||^2 as well.
+    Returns a device float64 tensor: 2 nv values (re, im interleaved) [+ ||w||^2]."""
+    import torch
+    nv, n = V.shape[0], w.numel()
+    prec = FP64 if V.dtype == torch.complex128 else FP32_MIXED
+    L = lib()
+    ws = int(L.gbprop_block_inner_product_workspace(n, nv))
+    work = torch.empty(ws, dtype=torch.uint8, device=V.device)
+    out = torch.empty(2 * nv + (1 if want_norm else 0), dtype=torch.float64, device=V.device)
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    check(L.gbprop_block_inner_product(prec, ptr(V), n, nv, ptr(w), int(bool(want_norm)), ptr(out), ptr(work), ws,
+                                       C.c_void_p(st)))
+    return out
+
+
 def launch_count():
     return int(lib().gbprop_launch_count())

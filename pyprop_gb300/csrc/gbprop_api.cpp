@@ -590,6 +590,29 @@ void set_inv_chunks(gbprop_ctx* h, bool wide) {
     }
 }
 
+// Use `nch` radial chunks for the solves of direction `dir`, staging the slices when they fit;
+// false if one CTA's share exceeds the shared-memory budget either way.
+bool set_inv_chunk_count(gbprop_ctx* h, int dir, int nch) {
+    InvTab& t = h->inv[dir];
+    const int n = h->nr, kd = h->kd, P = t.refine, w = t.w;
+    const bool mixed = h->prec != GBPROP_FP64;
+    const int chunk = std::max(4, ((n + nch - 1) / nch + 3) & ~3);
+    for (int stage = 1; stage >= 0; --stage) {
+        size_t mx = 0;
+        for (int q0 = 0; q0 < n; q0 += chunk) {
+            mx = std::max(mx, inv_smem_bytes(n, q0, chunk, P, w, kd, stage, 1));
+            if (mixed) mx = std::max(mx, inv_smem_bytes_mixed(n, q0, chunk, w, kd, stage));
+        }
+        if (mx <= (size_t)220 * 1024) {
+            t.chunk = chunk;
+            t.nchunks = (n + chunk - 1) / chunk;
+            t.stage = stage;
+            return true;
+        }
+    }
+    return false;
+}
+
 // Triangular solve of the Krylov precision: FP64-accurate (FP32 solve + FP64 refinement)
 // for the FP64 path, plain complex64 for the mixed path's basis.
 cudaError_t ksolve(gbprop_ctx* h, int dir, const void* in, int in_prec, void* out, int out_prec, void* vstore,
@@ -1280,6 +1303,31 @@ gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
         float ms = 0.f;
         GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         if (ms < best_ms) { best_ms = ms; best = v; }
+    }
+    // radial chunking of the overlap-factor solves (one problem spread over the GPU): time the
+    // Krylov-precision solve of each direction for 1..8 chunks and keep the fastest (batches keep
+    // the fewest chunks, other problems fill the GPU)
+    if (h->inv_ok && h->expm_max_cluster > 1) {
+        // finite non-zero input (0x3f bytes): a zero right-hand side ends the refinement early
+        GB_CUDA(cudaMemsetAsync(h->d_s, 0x3f, (size_t)h->N * h->kelem(), s));
+        for (int dir = 0; dir < 2; ++dir) {
+            const InvTab keep = h->inv[dir];
+            InvTab best_t = keep;
+            float best_s = 1e30f;
+            for (int nch = 1; nch <= 8; ++nch) {
+                if (nch > 1 && (h->nr + nch - 1) / nch < 32) break;
+                if (!set_inv_chunk_count(h, dir, nch)) continue;
+                for (int k = 0; k < 3; ++k) GB_LAUNCH(ksolve(h, dir, h->d_s, kp, h->d_y, kp, nullptr, kp, 0, 0));
+                GB_CUDA(cudaEventRecord(e0, s));
+                for (int k = 0; k < 10; ++k) GB_LAUNCH(ksolve(h, dir, h->d_s, kp, h->d_y, kp, nullptr, kp, 0, 0));
+                GB_CUDA(cudaEventRecord(e1, s));
+                GB_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best_s) { best_s = ms; best_t = h->inv[dir]; }
+            }
+            h->inv[dir] = best_t;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -99,3 +99,45 @@ def radial_overlap(problem):
     """Dense radial overlap matrix of a Problem."""
     rad = problem.psi.GetRepresentation().radial
     return _dense_from_diagonals(rad.overlap_diagonals(), rad.kd, rad.count)
+
+
+class DevicePopulations:
+    """Bound-state populations and ionisation of DEVICE wavefunctions, evaluated on the GPU
+    (the per-state projections of analysis.py:344-375 restated): the bra rows (S phi_b) are
+    formed once and kept on the device; every evaluation is one block inner product per 45
+    states (gbprop_block_inner_product, the Arnoldi step's inner-product kernel) and the
+    overlap-metric norm from the handle (gbprop_inner_product).  The eigenproblems giving the
+    states are solved once, at set-up, on the host.
+
+    states: (nb, nl*nr) S-normalised bound states (bound_states()); S: dense radial overlap;
+    handle: the propagator's libgbprop handle (for ||psi||_S)."""
+
+    def __init__(self, states, S, handle, device="cuda"):
+        import torch
+        states = np.asarray(states, dtype=np.complex128)
+        nb = states.shape[0]
+        nr = S.shape[0]
+        nl = states.shape[1] // nr
+        bra = (states.reshape(nb, nl, nr) @ S.T).reshape(nb, -1)        # (S phi_b) rows, S real symmetric
+        self.bra = torch.as_tensor(np.ascontiguousarray(bra)).to(device)
+        self.handle = handle
+        self.nb = nb
+
+    def populations(self, psi):
+        """|<phi_b|S|psi>|^2 (device float64 tensor, one per state)."""
+        import torch
+        from . import _native
+        w = psi.reshape(-1)
+        if w.dtype != torch.complex128:
+            w = w.to(torch.complex128)
+        out = []
+        for k0 in range(0, self.nb, 45):
+            r = _native.block_inner_product(self.bra[k0:k0 + 45], w)
+            out.append(r[0::2] ** 2 + r[1::2] ** 2)
+        return torch.cat(out)
+
+    def report(self, psi):
+        """As report(): populations, their sum ('bound'), norm - bound ('ionisation'), the norm."""
+        pops = self.populations(psi).cpu().numpy()
+        norm = self.handle.inner_product(psi, psi).real
+        return {"populations": pops, "bound": float(pops.sum()), "ionisation": float(norm - pops.sum()), "norm": norm}

@@ -99,7 +99,9 @@ def test_singular_pade_denominator(precision):
         with pytest.raises(_native.GbpropError) as e:
             h.synchronize()
         assert e.value.status == ELU
-        # the counters' accessor reports it as well (pAMP's GetOperatorCount path)
+        # the counters' accessor reports it as well (pAMP's GetOperatorCount path); the failed
+        # step left psi undefined (as the reference's throw does), so start from psi0 again
+        prob.psi.SetData(psi0)
         prob.AdvanceStep()
         with pytest.raises(_native.GbpropError) as e:
             prob.Propagator.PampWrapper.GetOperatorCount()

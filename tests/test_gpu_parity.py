@@ -223,7 +223,7 @@ def test_500_step_workload_vs_oracle():
                                 "hydrogen_velocity_small.ini"))
     prob = pp.Problem(conf)
     prob.SetupStep()
-    assert rel(prob.psi.GetDataNumpy(), g["psi0"]) == 0.0
+    assert rel(prob.psi.GetDataNumpy(), g["psi0"]) == 0.0     # the seeded start, normalised exactly
     assert np.allclose(scalings_for(prob, 500), g["scalings"], rtol=0, atol=0)
     for _ in prob.Advance(5):
         pass

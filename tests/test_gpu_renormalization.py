@@ -65,3 +65,21 @@ def test_inner_product_and_energy_vs_dense():
     psi = prob.psi.GetDataNumpy().ravel()
     e_want = (np.vdot(psi, H @ psi) / np.vdot(psi, S @ psi)).real
     assert abs(prob.GetEnergyExpectationValue() - e_want) < 1e-11 * abs(e_want)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
+def test_device_populations_vs_host(precision):
+    """Bound-state populations and ionisation evaluated on the GPU against the host restatement."""
+    import torch
+    from pyprop_gb300 import observables as ob
+    prob = make_problem(maxl=3, xsize=30, m=10, precision=precision)
+    states, _, _ = ob.problem_bound_states(prob)
+    S = ob.radial_overlap(prob)
+    prob.AdvanceSteps(5)
+    psi = prob.psi.GetData()
+    dev = ob.DevicePopulations(states, S, prob.Propagator.Handle())
+    got = dev.report(psi)
+    want = ob.report(prob.psi.GetDataNumpy().astype(np.complex128), states, S)
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert np.abs(got["populations"] - want["populations"]).max() < tol
+    assert abs(got["ionisation"] - want["ionisation"]) < tol and abs(got["norm"] - want["norm"]) < tol
