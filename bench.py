@@ -417,7 +417,7 @@ def run_batch(args, rank, world, local):
     prec = _native.FP64 if args.precision == "fp64" else _native.FP32_MIXED
     t0 = time.perf_counter()
     # one seeded batch; rank r advances its share of it (greedy bin-packing by per-step work)
-    full = random_batch(args.batch_size, seed=20261204)
+    full = random_batch(args.batch_size, seed=20261204, setup="gpu")   # radial matrices formed on the GPU
     mine = shard(full, world)[rank]
     probs = [full[i] for i in mine]
     bp = BatchPropagator(probs, precision=prec, autotune=True, device=device)

@@ -300,6 +300,23 @@ gbprop_status gbprop_block_inner_product(int precision, const void* V, long n, i
 gbprop_status gbprop_block_inner_product_noalloc(int precision, const void* V, long n, int nv, const void* w,
                                                  int want_norm, double* out, void* stream);
 
+/* Radial TensorPotential set-up on the GPU (TensorPotentialGenerator's B-spline projection,
+ * pyprop/tensorpotential/TensorPotentialGenerator.py:72-256 -> RepresentPotentialInBasisBSpline,
+ * core/tensorpotential/basis_bspline.h:10-48 -> BSpline::BSplineGlobalOverlapIntegral,
+ * core/transform/bspline/bspline.cpp:373-467; overlap Cholesky, overlapmatrix.cpp:9-104).
+ * For a B-spline basis of `order` on `knots` (nknots values; n = nknots - order splines), with the
+ * Gauss-Legendre rule (nodes, weights on [-1, 1], nquad points) on every interval of
+ * `breakpoints`, forms nmat band matrices M_m(i, j) = <B_i| f_m |d^deriv[m] B_j>, f_m(r) = coef[m]
+ * (fid 0), coef[m]/r (fid 1) or coef[m]/(2 r^2) (fid 2), with the reference's swap rule
+ * M(j, i) = (-1)^deriv M(i, j).  bands (HOST, nmat x (2 order - 1) x n): diagonal-major,
+ * bands[m][order - 1 + d][i] = M_m(i, i + d).  cholesky (HOST, order x n, or NULL): the upper
+ * Cholesky factor of matrix 0 (the overlap), cholesky[d][i] = U(i, i + d).  All HOST pointers;
+ * synchronous on `stream`; allocates its own device scratch. */
+gbprop_status gbprop_bspline_bands(int order, int nknots, const double* knots, int nbreak, const double* breakpoints,
+                                   int nquad, const double* nodes, const double* weights, int nmat, const int* fid,
+                                   const int* deriv, const double* coef, double* bands, double* cholesky,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

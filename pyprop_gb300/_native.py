@@ -106,6 +106,9 @@ _PROTOS = {
     "gbprop_block_inner_product_workspace": (C.c_size_t, [C.c_long, C.c_int]),
     "gbprop_block_inner_product": (C.c_int, [C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
+    "gbprop_bspline_bands": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                       C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]),
     "gbprop_block_inner_product_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p, C.c_int,
                                                      C.c_void_p, C.c_void_p]),
 }
@@ -349,6 +352,32 @@ def block_inner_product(V, w, want_norm=False, stream=None):
     check(L.gbprop_block_inner_product(prec, ptr(V), n, nv, ptr(w), int(bool(want_norm)), ptr(out), ptr(work), ws,
                                        C.c_void_p(st)))
     return out
+
+
+RADIAL_CONST, RADIAL_INV_R, RADIAL_INV_2R2 = 0, 1, 2
+
+
+def bspline_bands(bspline, terms, cholesky=False, stream=None):
+    """Band matrices <B_i| f |d^n B_j> of a basis.bspline.BSplineBasis on the GPU
+    (gbprop_bspline_bands).  terms: list of (function id, derivative order, coefficient) with
+    f = c, c / r or c / (2 r^2) (RADIAL_CONST, RADIAL_INV_R, RADIAL_INV_2R2).  Returns the list of
+    (2k - 1, n) diagonal arrays (D[k - 1 + d, i] = M(i, i + d), as BSplineBasis.band_diagonals)
+    and, with cholesky, the (k, n) upper Cholesky diagonals of the first matrix."""
+    import numpy as np
+    k, n = bspline.order, bspline.count
+    knots = np.ascontiguousarray(bspline.knots, dtype=np.float64)
+    bps = np.ascontiguousarray(bspline.breakpoints, dtype=np.float64)
+    nodes = np.ascontiguousarray(bspline.nodes, dtype=np.float64)
+    wts = np.ascontiguousarray(bspline.weights, dtype=np.float64)
+    fid = np.ascontiguousarray([t[0] for t in terms], dtype=np.int32)
+    der = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
+    coef = np.ascontiguousarray([t[2] for t in terms], dtype=np.float64)
+    out = np.zeros((len(terms), 2 * k - 1, n))
+    ch = np.zeros((k, n)) if cholesky else None
+    check(lib().gbprop_bspline_bands(k, len(knots), ptr(knots), len(bps), ptr(bps), len(nodes), ptr(nodes), ptr(wts),
+                                     len(terms), ptr(fid), ptr(der), ptr(coef), ptr(out), ptr(ch),
+                                     C.c_void_p(stream or 0)))
+    return [out[m] for m in range(len(terms))], ch
 
 
 def launch_count():

@@ -105,6 +105,15 @@ def gauss_legendre(order):
     return E[idx], 2.0 * V[0, idx] ** 2
 
 
+_GL = {}
+
+
+def _gauss_legendre_cached(order):
+    if order not in _GL:
+        _GL[order] = gauss_legendre(order)
+    return _GL[order]
+
+
 def scale_and_translate(x, a, b):
     """bspline.h:173-176: map [-1, 1] onto [a, b]."""
     return (x - 1.0) * (b - a) / 2.0 + b
@@ -125,17 +134,12 @@ class BSplineBasis:
         self.continuity = np.asarray(continuity, dtype=int)
         self.knots = knot_sequence(self.breakpoints, self.continuity, self.order)
         self.count = len(self.knots) - self.order
-        self.nodes, self.weights = gauss_legendre(self.order + int(quad_order_additional))
-        nb = len(self.breakpoints)
-        grid, gw, interval = [], [], []
-        for j in range(nb - 1):
-            a, b = self.breakpoints[j], self.breakpoints[j + 1]
-            for x, w in zip(self.nodes, self.weights):
-                grid.append(scale_and_translate(x, a, b))
-                gw.append((b - a) / 2.0 * w)
-                interval.append(j)
-        self.grid = np.array(grid)
-        self.grid_weights = np.array(gw)
+        self.nodes, self.weights = _gauss_legendre_cached(self.order + int(quad_order_additional))
+        # every interval's points in order (the same operations as scale_and_translate, per element)
+        a = self.breakpoints[:-1, None]
+        b = self.breakpoints[1:, None]
+        self.grid = ((self.nodes[None, :] - 1.0) * (b - a) / 2.0 + b).ravel()
+        self.grid_weights = ((b - a) / 2.0 * self.weights[None, :]).ravel()
         self._tables = None
 
     # -- evaluation (bspline.cpp:26-164) ---------------------------------

@@ -27,16 +27,38 @@ from .tensorpotential import diagonals_to_bandnh
 
 
 
+_ANGULAR = {}
+
+
+def _angular_dipole(lmax):
+    """Dipole selection-rule pairs of l = 0..lmax (m = 0) and the angular factors of the two
+    velocity-gauge terms, <l|cos|l'> and <l|d/dtheta-term|l'> by the theta quadrature of
+    RepresentPotentialInBasisReducedSphericalHarmonic (basis_reducedspherical.h:11-74); they
+    depend on lmax only, so a batch computes them once per distinct lmax."""
+    if lmax not in _ANGULAR:
+        tools = _sph.ReducedSphericalTools(lmax, 0)
+        pairs = _sph.selection_rule_pairs(tools)
+        cos_t = np.cos(tools.theta)[:, None]
+        ones = np.ones_like(cos_t)
+        c_cos = _sph.project_angular(tools, cos_t, pairs, 0)[:, 0]
+        c_der = _sph.project_angular(tools, ones, pairs, 1)[:, 0]
+        _ANGULAR[lmax] = (pairs, c_cos, c_der)
+    return _ANGULAR[lmax]
+
+
 class HydrogenProblem:
     """One hydrogen-like problem: l = 0..lmax (m = 0), nr B-splines of `order`
     on linear breakpoints over [0, rmax] (zero at both ends), H(t) = H0 + A(t) Hv,
     A(t) = A0 sin^2(pi t / T) (-cos(omega t)) on [0, T), A0 = E0 / omega."""
 
     def __init__(self, lmax, nr, rmax, order=7, omega=0.057, e0=0.05, cycles=8, m=20, dt=0.01, seed=0,
-                 charge=-1.0):
+                 charge=-1.0, setup="host"):
         self.lmax, self.nr, self.rmax, self.order = int(lmax), int(nr), float(rmax), int(order)
         self.omega, self.e0, self.cycles = float(omega), float(e0), float(cycles)
         self.m, self.dt, self.seed, self.charge = int(m), complex(dt), int(seed), float(charge)
+        if setup not in ("host", "gpu"):
+            raise ValueError("setup must be 'host' or 'gpu'")
+        self.setup = setup
         self.amplitude = self.e0 / self.omega
         self.pulse_duration = 2 * math.pi / self.omega * self.cycles
         # zero continuity at both ends: count = nbreak + order - 4 (interior multiplicity 1)
@@ -60,22 +82,25 @@ class HydrogenProblem:
         k = self.order - 1
         g = bs.grid
         n = self.nr
-        self.Sdiag = bs.band_diagonals(np.ones(len(g)), 0)
-        self.Ud = _bs.band_cholesky_upper_diagonals(self.Sdiag, k)
-        K2 = bs.band_diagonals(np.full(len(g), -0.5), 2)
-        C2 = bs.band_diagonals(1.0 / (2.0 * g * g), 0)
-        C1 = bs.band_diagonals(-1.0 / g, 0)
-        D1 = bs.band_diagonals(np.ones(len(g)), 1)
-        R1 = bs.band_diagonals(1.0 / g, 0)
+        if self.setup == "gpu":
+            # the six radial matrices and the overlap's Cholesky factor in one GPU call
+            # (gbprop_bspline_bands; the same quadrature and roundings as the host path below)
+            (self.Sdiag, K2, C2, C1, D1, R1), self.Ud = _native.bspline_bands(bs, [
+                (_native.RADIAL_CONST, 0, 1.0), (_native.RADIAL_CONST, 2, -0.5), (_native.RADIAL_INV_2R2, 0, 1.0),
+                (_native.RADIAL_INV_R, 0, -1.0), (_native.RADIAL_CONST, 1, 1.0), (_native.RADIAL_INV_R, 0, 1.0)],
+                cholesky=True)
+        else:
+            self.Sdiag = bs.band_diagonals(np.ones(len(g)), 0)
+            self.Ud = _bs.band_cholesky_upper_diagonals(self.Sdiag, k)
+            K2 = bs.band_diagonals(np.full(len(g), -0.5), 2)
+            C2 = bs.band_diagonals(1.0 / (2.0 * g * g), 0)
+            C1 = bs.band_diagonals(-1.0 / g, 0)
+            D1 = bs.band_diagonals(np.ones(len(g)), 1)
+            R1 = bs.band_diagonals(1.0 / g, 0)
         K2v, C2v, C1v = diagonals_to_bandnh(K2, k), diagonals_to_bandnh(C2, k), diagonals_to_bandnh(C1, k)
         ls = np.arange(self.nl, dtype=float)
         self.static = (K2v[None, :] + (ls * (ls + 1.0))[:, None] * C2v[None, :] + C1v[None, :]).astype(np.complex128)
-        tools = _sph.ReducedSphericalTools(self.lmax, 0)
-        self.pairs = _sph.selection_rule_pairs(tools)
-        cos_t = np.cos(tools.theta)[:, None]
-        ones = np.ones_like(cos_t)
-        c_cos = _sph.project_angular(tools, cos_t, self.pairs, 0)[:, 0]
-        c_der = _sph.project_angular(tools, ones, self.pairs, 1)[:, 0]
+        self.pairs, c_cos, c_der = _angular_dipole(self.lmax)
         q = self.charge
         Dv = diagonals_to_bandnh(D1, k)
         Rv = diagonals_to_bandnh(R1, k)
@@ -131,16 +156,17 @@ class HydrogenProblem:
 
 
 def random_batch(count=256, seed=20261204, lmax=(8, 64), nr=(200, 1500), rmax=(100.0, 400.0),
-                 omega=(0.04, 0.12), e0=(0.02, 0.1), msizes=(16, 24, 32), dt=0.01, order=7, cycles=8):
+                 omega=(0.04, 0.12), e0=(0.02, 0.1), msizes=(16, 24, 32), dt=0.01, order=7, cycles=8, setup="host"):
     """Seeded uneven batch: l_max ~ U{lmax}, Nr ~ U{nr}, r_max ~ U[rmax], omega ~ U[omega],
-    E0 ~ U[e0], m in msizes."""
+    E0 ~ U[e0], m in msizes.  setup = "gpu" forms the radial matrices on the GPU."""
     rng = np.random.default_rng(seed)
     probs = []
     for p in range(count):
         probs.append(HydrogenProblem(
             lmax=int(rng.integers(lmax[0], lmax[1] + 1)), nr=int(rng.integers(nr[0], nr[1] + 1)),
             rmax=float(rng.uniform(*rmax)), order=order, omega=float(rng.uniform(*omega)),
-            e0=float(rng.uniform(*e0)), cycles=cycles, m=int(rng.choice(msizes)), dt=dt, seed=seed + 1 + p))
+            e0=float(rng.uniform(*e0)), cycles=cycles, m=int(rng.choice(msizes)), dt=dt, seed=seed + 1 + p,
+            setup=setup))
     return probs
 
 

@@ -16,7 +16,9 @@ ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbprop.so")
 SOURCES = ["gbprop_kernels.cu", "gbprop_solve.cu", "gbprop_cgs.cu", "gbprop_expm.cu", "gbprop_api.cpp",
-           "gbprop_noalloc.cu"]
+           "gbprop_noalloc.cu", "gbprop_setup.cu"]
+# per-file flags: the set-up kernels reproduce the host restatement's roundings (no FMA contraction)
+EXTRA = {"gbprop_setup.cu": ["-fmad=false"]}
 HEADERS = ["gbprop_internal.h", "gbprop_device.cuh", os.path.join(ROOT, "include", "gbprop.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -48,7 +50,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _newer(obj, [path] + hdrs):
             lang = [] if src.endswith(".cu") else ["-x", "cu"]
             cmd = [nvcc] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-                                   "-I" + os.path.join(ROOT, "include"), "-c"] + lang + [path, "-o", obj]
+                                   "-I" + os.path.join(ROOT, "include"), "-c"] + EXTRA.get(src, []) + lang + \
+                [path, "-o", obj]
             jobs.append(cmd)
 
     def run(cmd):
