@@ -32,5 +32,9 @@ def GaussianRandomState(psi, conf):
     rng = np.random.default_rng(seed)
     c = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
     rad = repr_.radial
-    n2 = overlap_norm2_exact(c, rad.overlap_diagonals(), rad.kd)
-    psi.SetData(c / math.sqrt(n2))
+    nrm = math.sqrt(overlap_norm2_exact(c, rad.overlap_diagonals(), rad.kd))
+    # real divisions per component (complex division by a real differs between numpy builds)
+    out = np.empty(shape, dtype=np.complex128)
+    out.real = c.real / nrm
+    out.imag = c.imag / nrm
+    psi.SetData(out)
