@@ -265,6 +265,8 @@ extern "C" gbprop_status gbprop_bspline_bands(int order, int nknots, const doubl
         (const double*)d_wg.p, (const int*)d_first.p, (const double*)d_tab.p, (const int*)d_span.p, (double*)d_out.p);
     int info = 0;
     if (cholesky) {
+        e = cudaMemsetAsync(d_ud.p, 0, (size_t)k * n * 8, s);      // U(i, i+d) = 0 beyond the matrix
+        if (e) { set_last_error(cudaGetErrorString(e)); return GBPROP_ECUDA; }
         count_launch();
         k_band_cholesky<<<1, 32, 0, s>>>(n, kb, (const double*)d_out.p, (double*)d_ud.p, (int*)d_info.p);
         e = cudaMemcpyAsync(cholesky, d_ud.p, (size_t)k * n * 8, cudaMemcpyDeviceToHost, s);

@@ -223,7 +223,11 @@ def test_500_step_workload_vs_oracle():
                                 "hydrogen_velocity_small.ini"))
     prob = pp.Problem(conf)
     prob.SetupStep()
-    assert rel(prob.psi.GetDataNumpy(), g["psi0"]) == 0.0     # the seeded start, normalised exactly
+    # the seeded start; its overlap-metric normalisation depends on the Gauss-Legendre nodes, which
+    # the host's LAPACK (eigh) forms to a few ulps differently across machines -- start from the
+    # fixture's coefficients so that both sides propagate the same numbers
+    assert rel(prob.psi.GetDataNumpy(), g["psi0"]) < 1e-15
+    prob.psi.SetData(g["psi0"])
     assert np.allclose(scalings_for(prob, 500), g["scalings"], rtol=0, atol=0)
     for _ in prob.Advance(5):
         pass

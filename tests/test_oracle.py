@@ -197,7 +197,8 @@ def test_oracle_reproduces_large_fixture():
                                 "hydrogen_velocity_large.ini"))
     prob = pp.Problem(conf, device="cpu")
     prob.SetupWavefunction()
-    assert np.array_equal(prob.psi.GetDataNumpy().astype(np.complex128), g["psi0"])
+    x = prob.psi.GetDataNumpy().astype(np.complex128)
+    assert np.linalg.norm(x - g["psi0"]) / np.linalg.norm(x) < 1e-15    # the seeded start (host LAPACK may differ by ulps)
     op = orc.Operator.from_problem(prob)
     m, dt = int(g["m"]), complex(g["dt"])
     psi, _ = op.advance(g["gs0"], m, dt, g["scalings"][:20])
