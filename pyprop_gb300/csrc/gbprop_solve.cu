@@ -536,8 +536,8 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                             }
                         }
                         const double2 b = bq[q];
-                        const float bhx = (float)b.x, bhy = (float)b.y;
-                        const float blx = (float)(b.x - (double)bhx), bly = (float)(b.y - (double)bhy);
+                        const float bhx = d2f_fast(b.x), bhy = d2f_fast(b.y);
+                        const float blx = d2f_fast(b.x - f2d_fast(bhx)), bly = d2f_fast(b.y - f2d_fast(bhy));
                         float s_, e_;
                         two_sum(bhx, -hr, s_, e_);
                         v.x = __fadd_rn(s_, __fadd_rn(e_, __fsub_rn(blx, lr)));
@@ -550,8 +550,8 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                 for (int q = tid; q < Rk; q += kInvThreads) {
                     const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
                     double2 x = xq[q];
-                    x.x += (double)f.x;
-                    x.y += (double)f.y;
+                    x.x += f2d_fast(f.x);
+                    x.y += f2d_fast(f.y);
                     xq[q] = x;
                 }
                 __syncthreads();
@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                 if (q < Rr) {
                     double2 r = rsrc[q];
                     if (scaled) { r.x *= sdown; r.y *= sdown; }
-                    v = make_float2((float)r.x, (float)r.y);
+                    v = make_float2(d2f_fast(r.x), d2f_fast(r.y));
                 }
                 r32[q] = v;
             }
@@ -604,8 +604,8 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
             for (int q = tid; q < Rk; q += kInvThreads) {
                 const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
                 double2 x = xq[q];
-                if (scaled) { x.x = fma((double)f.x, sup, x.x); x.y = fma((double)f.y, sup, x.y); }
-                else { x.x += (double)f.x; x.y += (double)f.y; }
+                if (scaled) { x.x = fma(f2d_fast(f.x), sup, x.x); x.y = fma(f2d_fast(f.y), sup, x.y); }
+                else { x.x += f2d_fast(f.x); x.y += f2d_fast(f.y); }
                 xq[q] = x;
                 if (k == 0) x0f[q] = f;                  // x0 = f exactly when unscaled
             }
@@ -695,8 +695,8 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
                 const TI t = in[base + p];
                 double2 b = make_double2((double)t.x, (double)t.y);
                 if (scale_mode) { b.x *= sc; b.y *= sc; }
-                hi = make_float2((float)b.x, (float)b.y);
-                lo = make_float2((float)(b.x - (double)hi.x), (float)(b.y - (double)hi.y));
+                hi = make_float2(d2f_fast(b.x), d2f_fast(b.y));
+                lo = make_float2(d2f_fast(b.x - f2d_fast(hi.x)), d2f_fast(b.y - f2d_fast(hi.y)));
                 if (q < cl) {
                     if (vstore) vstore[base + p] = conv<TV>(b);
                     if (v0s) v0s[base + p] = make_float4(hi.x, hi.y, lo.x, lo.y);
