@@ -285,8 +285,10 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
                     ai1 = fma(a[d], v.y, ai1);
                 }
                 const T ar = ar0 + ar1, ai = ai0 + ai1;
-                yr[e] += Cr * ar - Ci * ai;
-                yi[e] += Cr * ai + Ci * ar;
+                // a term's factor is real or imaginary (one part of a potential): skip the other
+                if (Ci == T(0)) { yr[e] = fma(Cr, ar, yr[e]); yi[e] = fma(Cr, ai, yi[e]); }
+                else if (Cr == T(0)) { yr[e] = fma(-Ci, ai, yr[e]); yi[e] = fma(Ci, ar, yi[e]); }
+                else { yr[e] += Cr * ar - Ci * ai; yi[e] += Cr * ai + Ci * ar; }
             }
         }
     }
@@ -378,8 +380,9 @@ __global__ void __launch_bounds__(THREADS) k_band_apply_l1(BandOp<T> op, const c
                 else { ar0 = fma(a, v[d].x, ar0); ai0 = fma(a, v[d].y, ai0); }
             }
             const T ar = ar0 + ar1, ai = ai0 + ai1;
-            yr += Cr * ar - Ci * ai;
-            yi += Cr * ai + Ci * ar;
+            if (Ci == T(0)) { yr = fma(Cr, ar, yr); yi = fma(Cr, ai, yi); }
+            else if (Cr == T(0)) { yr = fma(-Ci, ai, yr); yi = fma(Ci, ar, yi); }
+            else { yr += Cr * ar - Ci * ai; yi += Cr * ai + Ci * ar; }
         }
     }
     if (active) y[(size_t)l * nr + i] = mk<T>(yr + zr, yi + zi);

@@ -605,6 +605,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                 const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
                 double2 x = xq[q];
                 if (scaled) { x.x = fma(f2d_fast(f.x), sup, x.x); x.y = fma(f2d_fast(f.y), sup, x.y); }
+                else if (k == 0) x = make_double2(f2d_fast(f.x), f2d_fast(f.y));   // x was 0: no add
                 else { x.x += f2d_fast(f.x); x.y += f2d_fast(f.y); }
                 xq[q] = x;
                 if (k == 0) x0f[q] = f;                  // x0 = f exactly when unscaled
