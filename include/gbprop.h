@@ -203,12 +203,28 @@ gbprop_status gbprop_time_step(gbprop_handle h, void* psi, const double* scaling
  *                            (the launch records the timeout and returns: GBPROP_ETIMEOUT)
  *   GBPROP_DEBUG_INJECT_LU   value != 0: every Pade solve reports a zero pivot, as zgetrf's
  *                            info != 0 in pamp.h:544-550 (GBPROP_ELU); 0 clears it
+ *   GBPROP_DEBUG_ROUND_MATVEC precision probe of FP64 handles, bits of value: 1 = the band
+ *                            matvec's outputs are rounded to complex64; 2 = the outputs of the
+ *                            Arnoldi loop's solves and of the Gram-Schmidt update are too.  1
+ *                            measures what complex64 matvec outputs alone cost a propagation, 3
+ *                            what complex64 storage of every Arnoldi vector costs (the FP32-mixed
+ *                            path's storage, with FP64 arithmetic); 0 clears it
  * Synchronises the handle's stream. */
 typedef enum {
     GBPROP_DEBUG_WAIT_LIMIT = 0,
-    GBPROP_DEBUG_INJECT_LU = 1
+    GBPROP_DEBUG_INJECT_LU = 1,
+    GBPROP_DEBUG_ROUND_MATVEC = 2
 } gbprop_debug_key;
 gbprop_status gbprop_debug_set(gbprop_handle h, int key, long long value);
+
+/* Precision probe of the Hessenberg exponentials, no counterpart in the reference: runs one
+ * exponential of the handle on a HOST Hessenberg matrix H (m x m complex128 row-major, unscaled,
+ * m = krylov_basis_size) at time step dt and returns y = exp(-i dt H) e1 (HOST, 2m doubles) and the
+ * scaling order.  form: 0 = the FP64 Pade kernel, 1 = the double-float Pade kernel of the
+ * FP32-mixed path, 2 = the eigenvector exponential.  Synchronous; overwrites the handle's
+ * Hessenberg buffer (as a step does). */
+gbprop_status gbprop_debug_expm(gbprop_handle h, const double* H, double dt_re, double dt_im, int form, double* y,
+                                int* scaling_order);
 
 /* Statistics of one gbprop_expokit_advance call (Expokit's zgexpv diagnostics). */
 typedef struct {

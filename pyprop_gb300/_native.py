@@ -23,6 +23,7 @@ STORAGE_IDENT = 1
 STORAGE_SIMP = 2
 DEBUG_WAIT_LIMIT = 0
 DEBUG_INJECT_LU = 1
+DEBUG_ROUND_MATVEC = 2
 
 
 class GbpropError(RuntimeError):
@@ -92,6 +93,8 @@ _PROTOS = {
     "gbprop_get_hessenberg": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gbprop_synchronize": (C.c_int, [C.c_void_p]),
     "gbprop_debug_set": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong]),
+    "gbprop_debug_expm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p,
+                                    C.POINTER(C.c_int)]),
     "gbprop_time_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                    C.POINTER(StepTimers)]),
     "gbprop_tensor_multiply_bandnh": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double,
@@ -276,6 +279,17 @@ class Handle:
         out["total_ms"] = t.total_ms
         out["launches"] = t.launches
         return out
+
+    def debug_expm(self, H, dt, form):
+        """y = exp(-i dt H) e1 by one of the handle's exponential kernels (0 FP64 Pade, 1 double-float
+        Pade, 2 eigenvector) on a host Hessenberg matrix; returns (y, scaling order)."""
+        import numpy as np
+        Hc = np.ascontiguousarray(H, dtype=np.complex128)
+        y = np.zeros(self.m, dtype=np.complex128)
+        so = C.c_int()
+        dt = complex(dt)
+        check(lib().gbprop_debug_expm(self._h, ptr(Hc), dt.real, dt.imag, int(form), ptr(y), C.byref(so)))
+        return y, so.value
 
     def debug_set(self, key, value):
         """Test hooks of the failure paths (DEBUG_WAIT_LIMIT, DEBUG_INJECT_LU; see gbprop.h)."""

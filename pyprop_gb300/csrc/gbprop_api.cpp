@@ -678,6 +678,9 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
     // the fused form hands beta to the next solve and (complex64) reads the split first vector:
     // both only the inverse-band solve provides
     const bool fused = h->cgs_grid > 0 && !dorth && h->expm_max_cluster > 1 && h->inv_ok;
+    // the FP32-pair split of a complex64 basis's FP64 first vector, written by the inverse-band
+    // solve of that vector: read by both Gram-Schmidt forms instead of the FP64 copy
+    float4* v0s = (h->d_v0s && h->inv_ok) ? (float4*)h->d_v0s : nullptr;
     if (fused) GB_CUDA(cudaMemsetAsync(h->d_gridbar, 0, 2 * sizeof(unsigned), s));
     // beta0 = ||x||
     GB_LAUNCH(launch_norm(0, h->d_x, N, h->d_partials, h->d_counter, h->d_ctrl, s));
@@ -692,7 +695,7 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
         const void* bpart = nullptr;
         if (fused && J > 0) bpart = (const char*)h->d_cgs_part + (size_t)J * h->cgs_grid * 16;
         if (J == 0 && h->d_v0)
-            GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, h->d_v0, 0, 1, 1, fused ? h->d_v0s : nullptr));
+            GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, h->d_v0, 0, 1, 1, v0s));
         else
             GB_LAUNCH(ksolve(h, 0, in, in_prec, h->d_s, kp, V + J * vbytes, kp, 1, 1, nullptr, bpart));
         tick(h, GBPROP_PHASE_SOLVE);
@@ -709,16 +712,16 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
             tick(h, GBPROP_PHASE_GRAM_SCHMIDT);
             continue;
         }
-        GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0,
+        GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, v0s, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0,
                                  dorth, s));
         if (J < m - 1 || dorth)
-            GB_LAUNCH(launch_cgs_update(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl,
+            GB_LAUNCH(launch_cgs_update(kp, V, h->d_v0, v0s, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl,
                                         dorth ? 2 : 0, s));
         if (dorth) {
             for (int pass = 0; pass < 3; ++pass) {
-                GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, 0,
+                GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, v0s, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, 0,
                                          s));
-                GB_LAUNCH(launch_cgs_update(kp, V, h->d_v0, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1,
+                GB_LAUNCH(launch_cgs_update(kp, V, h->d_v0, v0s, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1,
                                             s));
             }
         }
@@ -1249,6 +1252,30 @@ gbprop_status gbprop_time_step(gbprop_handle h, void* psi, const double* scaling
     return device_errors(h, true);
 }
 
+gbprop_status gbprop_debug_expm(gbprop_handle h, const double* H, double dt_re, double dt_im, int form, double* y,
+                                int* scaling_order) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (!H || !y) return fail(GBPROP_EINVAL, "null argument");
+    if (form < 0 || form > 2) return fail(GBPROP_EINVAL, "form: 0 FP64 Pade, 1 double-float Pade, 2 eigenvector");
+    const int m = h->m;
+    gbprop_status st;
+    if ((st = ensure_sched(h, 1))) return st;
+    const double zero[kMaxTimeFuncs] = {0.0, 0.0, 0.0, 0.0};
+    SchedEntry se = sched_entry(zero, h->nfuncs, dt_re, dt_im);
+    cudaStream_t s = h->stream;
+    GB_CUDA(cudaMemcpyAsync(h->d_sched, &se, sizeof(se), cudaMemcpyHostToDevice, s));
+    GB_CUDA(cudaMemsetAsync(&h->d_ctrl->step, 0, sizeof(int), s));
+    GB_CUDA(cudaMemcpyAsync(h->d_H, H, (size_t)2 * m * m * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (form == 2) GB_LAUNCH(launch_expm_eig(h->d_ctrl, h->d_H, m, h->d_sched, s));
+    else GB_LAUNCH(launch_expm(h->d_ctrl, h->d_H, m, h->d_sched, h->expm_max_cluster, s, form));
+    int so = 0;
+    GB_CUDA(cudaMemcpyAsync(y, h->d_ctrl->y, (size_t)2 * m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaMemcpyAsync(&so, &h->d_ctrl->scaling_order, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    if (scaling_order) *scaling_order = so;
+    return device_errors(h, true);
+}
+
 gbprop_status gbprop_debug_set(gbprop_handle h, int key, long long value) {
     if (gbprop_status st = check_handle(h, true)) return st;
     if (key == GBPROP_DEBUG_WAIT_LIMIT) {
@@ -1256,6 +1283,9 @@ gbprop_status gbprop_debug_set(gbprop_handle h, int key, long long value) {
     } else if (key == GBPROP_DEBUG_INJECT_LU) {
         const int v = value ? 1 : 0;
         GB_CUDA(cudaMemcpyAsync(&h->d_ctrl->inject_lu, &v, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    } else if (key == GBPROP_DEBUG_ROUND_MATVEC) {
+        const int v = (int)(value & 3);
+        GB_CUDA(cudaMemcpyAsync(&h->d_ctrl->round_matvec, &v, sizeof(int), cudaMemcpyHostToDevice, h->stream));
     } else {
         return fail(GBPROP_EINVAL, "unknown debug key");
     }

@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
     __shared__ double hs[2 * (kMaxBasis + 1)];
     __shared__ double red[kFuseThreads / 32];
     if (ctrl->broken) return;                        // uniform: written only between launches
+    const bool rnd = ctrl->round_matvec & 2;        // precision probe (FP64 handles)
     const int nv = J + 1, G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long i0 = (long)b * chunk;
     const int cl = (int)max(0L, min((long)chunk, n - i0));
@@ -208,6 +209,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
             }
             r.x -= (sr0 + sr1);
             r.y -= (si0 + si1);
+            if (rnd) r = round_c64(r);
             w[i0 + i] = r;
             nrm = fma(r.x, r.x, nrm);
             nrm = fma(r.y, r.y, nrm);

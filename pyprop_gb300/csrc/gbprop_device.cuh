@@ -96,6 +96,13 @@ __device__ __forceinline__ void set_inv_beta(Ctrl* c, double beta) {
 // between FP32 and FP64 issues on the FP64 pipe at the rate of an FP64 FMA (measured: 628 vs
 // 528 G/s over all SMs, against 14 T/s for integer ops), so the FP64-accurate solve, which
 // converts every element several times, forms them from the bit patterns instead.
+// Precision probe of FP64 handles (Ctrl::round_matvec): a complex128 value rounded to
+// complex64, as the FP32-mixed path stores it.  Bit 0: band matvec outputs; bit 1: the
+// outputs of the Arnoldi loop's solves and of the Gram-Schmidt update.
+__device__ __forceinline__ double2 round_c64(double2 v) {
+    return make_double2((double)(float)v.x, (double)(float)v.y);
+}
+
 //   d2f_fast: round to nearest even, as (float)d for results in FP32's normal range; results
 //             below it are flushed to signed zero; overflow gives +-inf and NaN stays NaN.
 //   f2d_fast: exact, as (double)f, except that subnormal floats become signed zero.

@@ -76,7 +76,7 @@ __host__ __device__ inline size_t inv_smem_bytes(int n, int q0, int chunk, int P
     size_t b = (size_t)RB * 16;
     if (r64) b += (size_t)R0 * 16 + (size_t)RB * 16;
     if (stage) b += (size_t)(w + 1) * R0p * 4;
-    b += (size_t)(R0 + w) * 8;
+    b += (size_t)(R0 + w + 2) * 8;                  // r32 with the padding of the paired M product
     if (r64) b += (size_t)R0 * 8;
     return b;
 }
@@ -89,7 +89,7 @@ __host__ __device__ inline size_t inv_smem_bytes_mixed(int n, int q0, int chunk,
     const int R0p = (R0 + 3) & ~3;
     size_t b = 0;
     if (stage) b += (size_t)(w + 1) * R0p * 4 + (size_t)2 * (kd + 1) * R0p * 4;
-    b += (size_t)RB * 16 + (size_t)R0 * 8 + (size_t)(R0 + w) * 8;
+    b += (size_t)RB * 16 + (size_t)((R0 + 1) & ~1) * 8 + (size_t)(R0 + w + 2) * 8;
     return b;
 }
 
@@ -109,7 +109,7 @@ template <typename T> struct BandOp {
 };
 
 // Device control block of one handle.  Every field is written by kernels only, except
-// inject_lu and wait_limit (set by the host through gbprop_debug_set).
+// inject_lu, wait_limit and round_matvec (set by the host through gbprop_debug_set).
 struct Ctrl {
     int step;               // index of the current entry of the schedule array
     int broken;             // happy breakdown seen in the current step
@@ -121,6 +121,8 @@ struct Ctrl {
     int wait_timeout;       // a bounded device-side wait (bulk-copy staging, grid barrier) gave up
     int inject_lu;          // test hook: the next exponentials report a zero pivot (host-set)
     long long wait_limit;   // polls of a launch's first bounded wait: 0 = default, < 0 = give up at once
+    int round_matvec;       // precision probe (host-set): bit 0 band outputs, bit 1 solve and
+                            // Gram-Schmidt outputs of FP64 handles rounded to complex64
     int ro_go;              // re-orthogonalisation requested for the current vector
     int ro_count;           // re-orthogonalisation passes done for the current vector
     long long operator_count;
@@ -204,14 +206,17 @@ cudaError_t launch_renormalize(double2* x, long n, double* partials, unsigned* c
                                cudaStream_t s);
 // v0 (complex64 basis only, may be null): FP64 copy of the first basis vector, used in
 // place of V row 0 by the dot, the update and the combination.
-cudaError_t launch_cgs_dot(int prec, const void* V, const double2* v0, long n, int nv, const void* w,
-                           double* partials, unsigned* counter, Ctrl* ctrl, int mode, int want_norm, cudaStream_t s);
+// v0: the FP64 first vector of a complex64 basis; v0s: its FP32-pair split (hi, lo), read
+// instead when given (written by the inverse-band solve of that vector)
+cudaError_t launch_cgs_dot(int prec, const void* V, const double2* v0, const float4* v0s, long n, int nv,
+                           const void* w, double* partials, unsigned* counter, Ctrl* ctrl, int mode, int want_norm,
+                           cudaStream_t s);
 // Stateless block inner product into a caller buffer (out: 2nv doubles, + ||w||^2 when want_norm).
 size_t block_inner_scratch_doubles(long n, int nvals);
 cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const void* w, int want_norm, double* out,
                                double* partials, unsigned* counter, cudaStream_t s);
-cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, long n, int nv, void* w, double* partials,
-                              unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
+cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, const float4* v0s, long n, int nv, void* w,
+                              double* partials, unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
 // brk_tol: happy-breakdown threshold on the new basis norm (pAMP: sqrt(eps), pamp.h:79;
 // Expokit: 1e-7).
 cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol,

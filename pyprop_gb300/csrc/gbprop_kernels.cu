@@ -158,6 +158,16 @@ __host__ __device__ constexpr int band_threads(int v) {
 }
 __host__ __device__ constexpr int band_per(int v) { return v == 0 ? 2 : v == 1 ? 2 : v == 2 ? 4 : 1; }
 
+// Output element of the band matvec; the precision probe (Ctrl::round_matvec, FP64 handles)
+// rounds it to complex64 to measure what complex64 matvec outputs alone cost a propagation.
+template <typename T>
+__device__ __forceinline__ cx<T> band_out(T re, T im, const Ctrl* ctrl) {
+    if constexpr (sizeof(T) == sizeof(double)) {
+        if (ctrl && (ctrl->round_matvec & 1)) return mk<T>((double)(float)re, (double)(float)im);
+    }
+    return mk<T>(re, im);
+}
+
 // Term factor coef_t * (s if time-dependent) of term t, formed by one thread per CTA and
 // shared: FP64 (cr, ci) for the FP64 band, the FP32 pairs (Cr, Crl, Ci, Cil) for the
 // complex64 band.  Per thread this was ~10 FP64 instructions per term, a large share of
@@ -295,7 +305,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply(BandOp<T> op, const cx<T
 #pragma unroll
     for (int e = 0; e < PER; ++e) {
         const int i = i0 + tid + e * THREADS;
-        if (i < nr) y[(size_t)l * nr + i] = mk<T>(yr[e] + zr[e], yi[e] + zi[e]);
+        if (i < nr) y[(size_t)l * nr + i] = band_out<T>(yr[e] + zr[e], yi[e] + zi[e], ctrl);
     }
 }
 
@@ -385,7 +395,7 @@ __global__ void __launch_bounds__(THREADS) k_band_apply_l1(BandOp<T> op, const c
             else { yr += Cr * ar - Ci * ai; yi += Cr * ai + Ci * ar; }
         }
     }
-    if (active) y[(size_t)l * nr + i] = mk<T>(yr + zr, yi + zi);
+    if (active) y[(size_t)l * nr + i] = band_out<T>(yr + zr, yi + zi, ctrl);
 }
 
 template <typename T, int KB, int V>
@@ -573,9 +583,19 @@ cudaError_t launch_norm(int prec, const void* x, long n, double* partials, unsig
 // when ctrl is null.
 constexpr int kDotThreads = 256;
 
+// conj(vh + vl) * x accumulated as FP32 pairs (error-free products, low parts to first order)
+__device__ __forceinline__ void dot_acc_pair(float& rh, float& rl, float& ih, float& il, float2 vh, float2 vl,
+                                             float2 x) {
+    acc_prod(rh, rl, vh.x, vl.x, x.x);
+    acc_prod(rh, rl, vh.y, vl.y, x.y);
+    acc_prod(ih, il, vh.x, vl.x, x.y);
+    acc_prod(ih, il, -vh.y, -vl.y, x.x);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict__ V,
-                                                         const double2* __restrict__ v0, long n, int nv,
+                                                         const double2* __restrict__ v0,
+                                                         const float4* __restrict__ v0s, long n, int nv,
                                                          const cx<T>* __restrict__ w, double* partials,
                                                          unsigned* counter, Ctrl* ctrl, int mode, int want_norm,
                                                          double* hout, int epl) {
@@ -593,35 +613,44 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_dot(const cx<T>* __restrict
     double ar[4] = {0.0, 0.0, 0.0, 0.0}, ai[4] = {0.0, 0.0, 0.0, 0.0};
     int t = 0;
     if constexpr (sizeof(T) < sizeof(double)) {
-        if (!row64) {
+        if (!row64 || v0s) {
             // complex64 operands: error-free FP32 products and compensated FP32 sums (the
-            // result equals the FP64 dot to ~2^-48); FP64 only for the block reduction
+            // result equals the FP64 dot to ~2^-48); FP64 only for the block reduction.  The
+            // FP64 first vector enters as its FP32-pair split (hi, lo), no FP64 instruction
             float rh0 = 0.f, rl0 = 0.f, ih0 = 0.f, il0 = 0.f, rh1 = 0.f, rl1 = 0.f, ih1 = 0.f, il1 = 0.f;
+            auto vload = [&](long e, float2& vh, float2& vl) {
+                if (row64) {
+                    const float4 a = v0s[e];
+                    vh = make_float2(a.x, a.y);
+                    vl = make_float2(a.z, a.w);
+                } else {
+                    const C v = vk[e];
+                    vh = make_float2(v.x, v.y);
+                    vl = make_float2(0.f, 0.f);
+                }
+            };
             for (; t + 1 < epl; t += 2) {
                 const long ea = e0 + (long)t * kDotThreads, eb = ea + kDotThreads;
                 if (ea < n) {
-                    const C v = vk[ea], x = w[ea];
-                    acc_prod(rh0, rl0, v.x, 0.f, x.x);
-                    acc_prod(rh0, rl0, v.y, 0.f, x.y);
-                    acc_prod(ih0, il0, v.x, 0.f, x.y);
-                    acc_prod(ih0, il0, -v.y, 0.f, x.x);
+                    float2 vh, vl;
+                    vload(ea, vh, vl);
+                    const C x = w[ea];
+                    dot_acc_pair(rh0, rl0, ih0, il0, vh, vl, make_float2(x.x, x.y));
                 }
                 if (eb < n) {
-                    const C v = vk[eb], x = w[eb];
-                    acc_prod(rh1, rl1, v.x, 0.f, x.x);
-                    acc_prod(rh1, rl1, v.y, 0.f, x.y);
-                    acc_prod(ih1, il1, v.x, 0.f, x.y);
-                    acc_prod(ih1, il1, -v.y, 0.f, x.x);
+                    float2 vh, vl;
+                    vload(eb, vh, vl);
+                    const C x = w[eb];
+                    dot_acc_pair(rh1, rl1, ih1, il1, vh, vl, make_float2(x.x, x.y));
                 }
             }
             for (; t < epl; ++t) {
                 const long ea = e0 + (long)t * kDotThreads;
                 if (ea < n) {
-                    const C v = vk[ea], x = w[ea];
-                    acc_prod(rh0, rl0, v.x, 0.f, x.x);
-                    acc_prod(rh0, rl0, v.y, 0.f, x.y);
-                    acc_prod(ih0, il0, v.x, 0.f, x.y);
-                    acc_prod(ih0, il0, -v.y, 0.f, x.x);
+                    float2 vh, vl;
+                    vload(ea, vh, vl);
+                    const C x = w[ea];
+                    dot_acc_pair(rh0, rl0, ih0, il0, vh, vl, make_float2(x.x, x.y));
                 }
             }
             ar[0] = ((double)rh0 + (double)rl0) + ((double)rh1 + (double)rl1);
@@ -714,19 +743,20 @@ static void dot_shape(long n, int nvals, int* epl, int* nchunks) {
     *nchunks = (int)((n + (long)kDotThreads * e - 1) / ((long)kDotThreads * e));
 }
 
-cudaError_t launch_cgs_dot(int prec, const void* V, const double2* v0, long n, int nv, const void* w, double* partials,
-                           unsigned* counter, Ctrl* ctrl, int mode, int want_norm, cudaStream_t s) {
+cudaError_t launch_cgs_dot(int prec, const void* V, const double2* v0, const float4* v0s, long n, int nv,
+                           const void* w, double* partials, unsigned* counter, Ctrl* ctrl, int mode, int want_norm,
+                           cudaStream_t s) {
     count_launch();
     const int nvals = nv + ((want_norm && mode == 0) ? 1 : 0);
     int epl, nch;
     dot_shape(n, nvals, &epl, &nch);
     dim3 grid(nch, nvals);
     if (prec == 0)
-        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, nullptr, n, nv, (const double2*)w, partials,
-                                                       counter, ctrl, mode, want_norm, nullptr, epl);
+        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, nullptr, nullptr, n, nv, (const double2*)w,
+                                                       partials, counter, ctrl, mode, want_norm, nullptr, epl);
     else
-        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, v0, n, nv, (const float2*)w, partials, counter,
-                                                      ctrl, mode, want_norm, nullptr, epl);
+        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, v0, v0s, n, nv, (const float2*)w, partials,
+                                                      counter, ctrl, mode, want_norm, nullptr, epl);
     return cudaGetLastError();
 }
 
@@ -744,11 +774,11 @@ cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const vo
     dot_shape(n, nvals, &epl, &nch);
     dim3 grid(nch, nvals);
     if (prec == 0)
-        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, nullptr, n, nv, (const double2*)w, partials,
-                                                       counter, nullptr, 0, want_norm, out, epl);
+        k_cgs_dot<double><<<grid, kDotThreads, 0, s>>>((const double2*)V, nullptr, nullptr, n, nv, (const double2*)w,
+                                                       partials, counter, nullptr, 0, want_norm, out, epl);
     else
-        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, nullptr, n, nv, (const float2*)w, partials,
-                                                      counter, nullptr, 0, want_norm, out, epl);
+        k_cgs_dot<float><<<grid, kDotThreads, 0, s>>>((const float2*)V, nullptr, nullptr, n, nv, (const float2*)w,
+                                                      partials, counter, nullptr, 0, want_norm, out, epl);
     return cudaGetLastError();
 }
 
@@ -761,7 +791,8 @@ constexpr int kUpdThreads = 256;
 
 template <typename T>
 __global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restrict__ V,
-                                                            const double2* __restrict__ v0, long n, int nv,
+                                                            const double2* __restrict__ v0,
+                                                            const float4* __restrict__ v0s, long n, int nv,
                                                             cx<T>* __restrict__ w, double* partials,
                                                             unsigned* counter, Ctrl* ctrl, int mode) {
     using C = cx<T>;
@@ -782,15 +813,22 @@ __global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restr
     }
     __syncthreads();
     double acc[1] = {0.0};
+    float nh = 0.f, nl = 0.f;                      // ||w||^2 as an FP32 pair (complex64 basis)
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         T sr[4] = {0, 0, 0, 0}, si[4] = {0, 0, 0, 0};
         T cr = 0, ci = 0;                          // remainder sums (complex64 basis only)
         int k = 0;
         if (v0) {                                    // first vector kept in FP64: hi + lo parts
-            const double2 a = v0[i];
             const C hk = hs[0], hlk = hl[0];
-            const T ax = (T)a.x, ay = (T)a.y;
-            const T bx = (T)(a.x - (double)ax), by = (T)(a.y - (double)ay);
+            T ax, ay, bx, by;
+            if (v0s) {                               // its FP32-pair split (no FP64 instruction)
+                const float4 a = v0s[i];
+                ax = (T)a.x; ay = (T)a.y; bx = (T)a.z; by = (T)a.w;
+            } else {
+                const double2 a = v0[i];
+                ax = (T)a.x; ay = (T)a.y;
+                bx = (T)(a.x - (double)ax); by = (T)(a.y - (double)ay);
+            }
             sr[0] = fma(ax, hk.x, sr[0]);
             sr[0] = fma(-ay, hk.y, sr[0]);
             si[0] = fma(ax, hk.y, si[0]);
@@ -837,11 +875,19 @@ __global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restr
         C r = w[i];
         r.x -= ((sr[0] + sr[1]) + (sr[2] + sr[3])) + cr;
         r.y -= ((si[0] + si[1]) + (si[2] + si[3])) + ci;
+        if constexpr (!kSplit) {
+            if (ctrl->round_matvec & 2) r = round_c64(r);
+        }
         w[i] = r;
-        const double re = (double)r.x, im = (double)r.y;
-        acc[0] = fma(re, re, acc[0]);
-        acc[0] = fma(im, im, acc[0]);
+        if constexpr (kSplit) {
+            acc_prod(nh, nl, r.x, 0.f, r.x);
+            acc_prod(nh, nl, r.y, 0.f, r.y);
+        } else {
+            acc[0] = fma((double)r.x, (double)r.x, acc[0]);
+            acc[0] = fma((double)r.y, (double)r.y, acc[0]);
+        }
     }
+    if constexpr (kSplit) acc[0] = (double)nh + (double)nl;
     block_partials<1>(acc, 1, partials, kPStride, 0);
     if (is_last_block(counter)) {
         __shared__ double tot[1];
@@ -870,17 +916,17 @@ __global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restr
     }
 }
 
-cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, long n, int nv, void* w, double* partials,
-                              unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s) {
+cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, const float4* v0s, long n, int nv, void* w,
+                              double* partials, unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s) {
     count_launch();
     int blocks = (int)((n + kUpdThreads - 1) / kUpdThreads);
     if (blocks > grid_reduce_blocks() * 4) blocks = grid_reduce_blocks() * 4;
     if (prec == 0)
-        k_cgs_update<double><<<blocks, kUpdThreads, 0, s>>>((const double2*)V, nullptr, n, nv, (double2*)w, partials,
-                                                            counter, ctrl, mode);
+        k_cgs_update<double><<<blocks, kUpdThreads, 0, s>>>((const double2*)V, nullptr, nullptr, n, nv, (double2*)w,
+                                                            partials, counter, ctrl, mode);
     else
-        k_cgs_update<float><<<blocks, kUpdThreads, 0, s>>>((const float2*)V, v0, n, nv, (float2*)w, partials, counter,
-                                                           ctrl, mode);
+        k_cgs_update<float><<<blocks, kUpdThreads, 0, s>>>((const float2*)V, v0, v0s, n, nv, (float2*)w, partials,
+                                                           counter, ctrl, mode);
     return cudaGetLastError();
 }
 

@@ -370,36 +370,44 @@ cudaError_t launch_solve_ir(const void* tabf, const double* udp, int nrows, cons
 // slices of M and U~ arrive by bulk asynchronous copies (one mbarrier) while the threads
 // load the right-hand side.
 constexpr int kInvThreads = 512;
-// x (+)= M r32 for element q: FP32 products, four independent chains per component.
+// x (+)= M r32 for the elements q and q + 1 (q even; r32 16-byte aligned and readable up to
+// q + w + 1): FP32 products, two independent chains per component.  Every pair of r32
+// values is one 16-byte load and every pair of M entries one 8-byte load, each used for
+// both outputs -- 3 loads per 8 FMAs instead of 8.  With t = j for element q and t = j + 1
+// for element q + 1, r32[q + t] meets M[t][q] and M[t-1][q+1].
 template <bool STAGE>
-__device__ __forceinline__ float2 inv_apply(const float* mrow, size_t mstride, const float2* r32, int q, int w) {
-    float ar0 = 0.f, ai0 = 0.f, ar1 = 0.f, ai1 = 0.f, ar2 = 0.f, ai2 = 0.f, ar3 = 0.f, ai3 = 0.f;
-    int j = 0;
-    for (; j + 3 <= w; j += 4) {
-        float m0, m1, m2, m3;
-        if (STAGE) {
-            m0 = mrow[(size_t)j * mstride];
-            m1 = mrow[(size_t)(j + 1) * mstride];
-            m2 = mrow[(size_t)(j + 2) * mstride];
-            m3 = mrow[(size_t)(j + 3) * mstride];
-        } else {
-            m0 = __ldg(mrow + (size_t)j * mstride);
-            m1 = __ldg(mrow + (size_t)(j + 1) * mstride);
-            m2 = __ldg(mrow + (size_t)(j + 2) * mstride);
-            m3 = __ldg(mrow + (size_t)(j + 3) * mstride);
-        }
-        const float2 v0 = r32[q + j], v1 = r32[q + j + 1], v2 = r32[q + j + 2], v3 = r32[q + j + 3];
-        ar0 = fmaf(m0, v0.x, ar0); ai0 = fmaf(m0, v0.y, ai0);
-        ar1 = fmaf(m1, v1.x, ar1); ai1 = fmaf(m1, v1.y, ai1);
-        ar2 = fmaf(m2, v2.x, ar2); ai2 = fmaf(m2, v2.y, ai2);
-        ar3 = fmaf(m3, v3.x, ar3); ai3 = fmaf(m3, v3.y, ai3);
+__device__ __forceinline__ float2 inv_m2(const float* mrow, size_t mstride, int t) {
+    const float2* p = reinterpret_cast<const float2*>(mrow + (size_t)t * mstride);
+    return STAGE ? *p : __ldg(p);
+}
+
+template <bool STAGE>
+__device__ __forceinline__ float4 inv_apply2(const float* mrow, size_t mstride, const float2* r32, int q, int w) {
+    const float4* r4 = reinterpret_cast<const float4*>(r32 + q);
+    float a0r = 0.f, a0i = 0.f, b0r = 0.f, b0i = 0.f;   // element q: even / odd t
+    float a1r = 0.f, a1i = 0.f, b1r = 0.f, b1i = 0.f;   // element q + 1
+    float pm = 0.f;                                     // M[t-1][q+1] (none at t = 0)
+    int t = 0;
+    for (; t + 1 <= w; t += 2) {
+        const float4 rr = r4[t >> 1];                   // r[q+t], r[q+t+1]
+        const float2 m0 = inv_m2<STAGE>(mrow, mstride, t), m1 = inv_m2<STAGE>(mrow, mstride, t + 1);
+        a0r = fmaf(m0.x, rr.x, a0r); a0i = fmaf(m0.x, rr.y, a0i);
+        a1r = fmaf(pm, rr.x, a1r);   a1i = fmaf(pm, rr.y, a1i);
+        b0r = fmaf(m1.x, rr.z, b0r); b0i = fmaf(m1.x, rr.w, b0i);
+        b1r = fmaf(m0.y, rr.z, b1r); b1i = fmaf(m0.y, rr.w, b1i);
+        pm = m1.y;
     }
-    for (; j <= w; ++j) {
-        const float m0 = STAGE ? mrow[(size_t)j * mstride] : __ldg(mrow + (size_t)j * mstride);
-        const float2 v0 = r32[q + j];
-        ar0 = fmaf(m0, v0.x, ar0); ai0 = fmaf(m0, v0.y, ai0);
+    if (t <= w) {                                       // w even: t = w
+        const float4 rr = r4[t >> 1];
+        const float2 m0 = inv_m2<STAGE>(mrow, mstride, t);
+        a0r = fmaf(m0.x, rr.x, a0r); a0i = fmaf(m0.x, rr.y, a0i);
+        a1r = fmaf(pm, rr.x, a1r);   a1i = fmaf(pm, rr.y, a1i);
+        b1r = fmaf(m0.y, rr.z, b1r); b1i = fmaf(m0.y, rr.w, b1i);
+    } else {                                            // w odd: t = w + 1
+        const float2 rl = r32[q + t];
+        a1r = fmaf(pm, rl.x, a1r); a1i = fmaf(pm, rl.y, a1i);
     }
-    return make_float2((ar0 + ar1) + (ar2 + ar3), (ai0 + ai1) + (ai2 + ai3));
+    return make_float4(a0r + b0r, a0i + b0i, a1r + b1r, a1i + b1i);
 }
 
 template <int KD, bool R64, bool STAGE, typename TI, typename TO, typename TV>
@@ -426,8 +434,8 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
     if (R64) sp += (size_t)R0 * 16 + (size_t)RB * 16;
     float* Ms = reinterpret_cast<float*>(sp);
     if (STAGE) sp += (size_t)(w + 1) * R0p * 4;
-    float2* r32 = reinterpret_cast<float2*>(sp);
-    sp += (size_t)(R0 + w) * 8;
+    float2* r32 = reinterpret_cast<float2*>(sp);     // 16-byte aligned; 2 slots of padding
+    sp += (size_t)(R0 + w + 2) * 8;
     float2* x0f = reinterpret_cast<float2*>(sp);     // FP32 first iterate (exact in FP32)
 
     const float* Mg = tab.m + q0;
@@ -521,7 +529,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                 // (U~ = uh + ul, b = bh + bl; error-free products and sums).  Its relative error
                 // (~2^-48 |b| / |r|) is far below what this pass needs; the last pass uses an FP64
                 // residual.  No scaling: |b| has an FP32-safe exponent (checked at pass 0).
-                for (int q = tid; q < Rk + w; q += kInvThreads) {
+                for (int q = tid; q < Rk + w + 2; q += kInvThreads) {
                     float2 v = make_float2(0.f, 0.f);
                     if (q < Rr) {
                         float hr = 0.f, lr = 0.f, hi_ = 0.f, li = 0.f;
@@ -547,12 +555,18 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                     r32[q] = v;
                 }
                 __syncthreads();
-                for (int q = tid; q < Rk; q += kInvThreads) {
-                    const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
+                for (int q = 2 * tid; q < Rk; q += 2 * kInvThreads) {
+                    const float4 f = inv_apply2<STAGE>(mbase + q, mstride, r32, q, w);
                     double2 x = xq[q];
                     x.x += f2d_fast(f.x);
                     x.y += f2d_fast(f.y);
                     xq[q] = x;
+                    if (q + 1 < Rk) {
+                        x = xq[q + 1];
+                        x.x += f2d_fast(f.z);
+                        x.y += f2d_fast(f.w);
+                        xq[q + 1] = x;
+                    }
                 }
                 __syncthreads();
                 continue;
@@ -591,7 +605,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
             const bool scaled = e < -100 || e > 100;
             const double sdown = scaled ? ldexp(1.0, -e) : 1.0, sup = scaled ? ldexp(1.0, e) : 1.0;
             const double2* rsrc = k > 0 ? rq : bq;
-            for (int q = tid; q < Rk + w; q += kInvThreads) {
+            for (int q = tid; q < Rk + w + 2; q += kInvThreads) {
                 float2 v = make_float2(0.f, 0.f);
                 if (q < Rr) {
                     double2 r = rsrc[q];
@@ -601,21 +615,27 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_inv(InvTab tab, const TI*
                 r32[q] = v;
             }
             __syncthreads();
-            for (int q = tid; q < Rk; q += kInvThreads) {
-                const float2 f = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
-                double2 x = xq[q];
-                if (scaled) { x.x = fma(f2d_fast(f.x), sup, x.x); x.y = fma(f2d_fast(f.y), sup, x.y); }
-                else if (k == 0) x = make_double2(f2d_fast(f.x), f2d_fast(f.y));   // x was 0: no add
-                else { x.x += f2d_fast(f.x); x.y += f2d_fast(f.y); }
-                xq[q] = x;
-                if (k == 0) x0f[q] = f;                  // x0 = f exactly when unscaled
+            for (int q = 2 * tid; q < Rk; q += 2 * kInvThreads) {
+                const float4 f4 = inv_apply2<STAGE>(mbase + q, mstride, r32, q, w);
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    if (e == 1 && q + 1 >= Rk) break;
+                    const float2 f = e ? make_float2(f4.z, f4.w) : make_float2(f4.x, f4.y);
+                    double2 x = xq[q + e];
+                    if (scaled) { x.x = fma(f2d_fast(f.x), sup, x.x); x.y = fma(f2d_fast(f.y), sup, x.y); }
+                    else if (k == 0) x = make_double2(f2d_fast(f.x), f2d_fast(f.y));   // x was 0: no add
+                    else { x.x += f2d_fast(f.x); x.y += f2d_fast(f.y); }
+                    xq[q + e] = x;
+                    if (k == 0) x0f[q + e] = f;          // x0 = f exactly when unscaled
+                }
             }
             if (k == 0) x0_exact = !scaled && e > -60 && e < 60;   // the FP32-pair residual stays normal
             __syncthreads();
         }
+        const bool rnd = check_broken && (ctrl->round_matvec & 2);   // precision probe, Arnoldi solves
         for (int q = tid; q < cl; q += kInvThreads) {
             const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-            out[base + p] = conv<TO>(xq[q]);
+            out[base + p] = conv<TO>(rnd ? round_c64(xq[q]) : xq[q]);
         }
     }
 }
@@ -650,8 +670,8 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
     if (STAGE) sp += (size_t)(w + 1) * R0p * 4 + (size_t)2 * (KD + 1) * R0p * 4;
     float2* bh = reinterpret_cast<float2*>(sp);
     float2* bl = bh + RB;
-    float2* x0 = bl + RB;
-    float2* r32 = x0 + R0;
+    float2* x0 = bl + RB;                          // 16-byte aligned
+    float2* r32 = x0 + ((R0 + 1) & ~1);            // 16-byte aligned; 2 slots of padding
 
     const float* Mg = tab.m + q0;
     const float* Uhg = tab.uh + q0;
@@ -689,7 +709,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
     if constexpr (kWide) {
         // the FP64 first vector (once per step): scaled in FP64, kept as hi + lo
         const double sc = scale_mode ? ctrl->inv_beta : 1.0;
-        for (int q = tid; q < R0 + w; q += kInvThreads) {
+        for (int q = tid; q < R0 + w + 2; q += kInvThreads) {
             float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
             if (q < RB) {
                 const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
@@ -727,7 +747,7 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
         if (scale_mode && !late) { sh = ctrl->inv_beta_f[0]; sl = ctrl->inv_beta_f[1]; }
         const int t0 = late ? tid - 32 : tid, tstep = late ? kInvThreads - 32 : kInvThreads;
         if (t0 >= 0)
-            for (int q = t0; q < R0 + w; q += tstep) {
+            for (int q = t0; q < R0 + w + 2; q += tstep) {
                 float2 hi = make_float2(0.f, 0.f);
                 if (q < RB) {
                     const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
@@ -764,7 +784,11 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
         if (STAGE) mbar_wait0(&s_bar);             // let copies in flight land before exit
         return;
     }
-    for (int q = tid; q < R0; q += kInvThreads) x0[q] = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
+    for (int q = 2 * tid; q < R0; q += 2 * kInvThreads) {
+        const float4 f = inv_apply2<STAGE>(mbase + q, mstride, r32, q, w);
+        if (q + 1 < R0) *reinterpret_cast<float4*>(x0 + q) = f;
+        else x0[q] = make_float2(f.x, f.y);
+    }
     __syncthreads();
     const int Rr = min(n - q0, cl + w);
     for (int q = tid; q < cl + w; q += kInvThreads) {
@@ -790,11 +814,14 @@ __global__ void __launch_bounds__(kInvThreads) k_solve_mixed(InvTab tab, const T
         r32[q] = r;
     }
     __syncthreads();
-    for (int q = tid; q < cl; q += kInvThreads) {
-        const float2 d = inv_apply<STAGE>(mbase + q, mstride, r32, q, w);
-        const float2 x = x0[q];
-        const int p = dir ? (n - 1 - (q0 + q)) : (q0 + q);
-        out[base + p] = make_float2(__fadd_rn(x.x, d.x), __fadd_rn(x.y, d.y));
+    for (int q = 2 * tid; q < cl; q += 2 * kInvThreads) {
+        const float4 d = inv_apply2<STAGE>(mbase + q, mstride, r32, q, w);
+        float2 x = x0[q];
+        out[base + (dir ? (n - 1 - (q0 + q)) : (q0 + q))] = make_float2(__fadd_rn(x.x, d.x), __fadd_rn(x.y, d.y));
+        if (q + 1 < cl) {
+            x = x0[q + 1];
+            out[base + (dir ? (n - 2 - (q0 + q)) : (q0 + q + 1))] = make_float2(__fadd_rn(x.x, d.z), __fadd_rn(x.y, d.w));
+        }
     }
 }
 

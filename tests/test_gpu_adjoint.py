@@ -100,3 +100,48 @@ def test_autograd_two_forward_calls_then_backward_on_the_first():
     assert rel(g1, g2) > 1e-3                       # the two calls have different gradients
     assert rel(x1.grad.numpy(), g1) < 1e-13
     assert rel(x2.grad.numpy(), g2) < 1e-13
+
+
+def test_adjoint_at_reduced_size_vs_central_differences_and_taylor_remainder():
+    """l = 0..15 x 200 B-splines (r_max = 100), m = 20, 1000 steps of dt = 0.002, 64 field
+    samples: the gradient of the ground-state survival probability against central differences
+    and through the Taylor remainder O(c + h d) - O(c) - h g.d, which must fall as h^2.
+
+    The smallest useful difference step is set by the forward map's rounding: the 1000 steps
+    leave O with noise of ~1e-13 between nearby field values (not smooth below that), which is
+    ~4e-5 of max|g| * 2h at h = 1e-6 and ~1e-7 at h = 1e-4."""
+    from pyprop_gb300.adjoint import AdjointPropagator, bound_states
+    from pyprop_gb300.batch import HydrogenProblem
+    prob = HydrogenProblem(lmax=15, nr=200, rmax=100.0, m=20, dt=0.002, seed=20261205)
+    states, _, _ = bound_states(prob)
+    ground = states[:1]
+    psi0 = states[0].reshape(prob.nl, prob.nr)
+    rng = np.random.default_rng(20261205)
+    c = rng.normal(0.05, 0.01, NSAMPLES)
+    ap = AdjointPropagator(prob, 1000, NSAMPLES, checkpoint=50)
+    g, _ = ap.gradient(ap.forward(psi0, c), ground)
+    scale = float(np.abs(g).max())
+
+    def O(x):
+        return ap.observable(ap.forward(psi0, x, keep=False), ground)
+
+    h = 1e-4
+    for k in (5, 31, 58):
+        cp, cm = c.copy(), c.copy()
+        cp[k] += h
+        cm[k] -= h
+        fd = (O(cp) - O(cm)) / (2 * h)
+        print("sample %d: central difference %.12e, adjoint %.12e" % (k, fd, g[k]))
+        assert abs(fd - g[k]) <= 1e-5 * scale, (k, fd, g[k])
+    d = rng.standard_normal(NSAMPLES)
+    O0, gd = O(c), float(g @ d)
+    r1, r2 = [], []
+    for hh in (1e-2, 5e-3, 2.5e-3):
+        Oh = O(c + hh * d)
+        r1.append(abs(Oh - O0))
+        r2.append(abs(Oh - O0 - hh * gd))
+    print("Taylor remainders: without gradient", r1, "with gradient", r2)
+    for a, b in zip(r2, r2[1:]):
+        assert 3.0 < a / b < 5.0                    # second order: halving h divides by 4
+    for a, b in zip(r1, r1[1:]):
+        assert 1.6 < a / b < 2.4                    # first order without the gradient term

@@ -24,11 +24,20 @@ def _problem(precision):
     return prob
 
 
-def _run(prob, psi0, nsteps):
+def _run(prob, psi0, nsteps, round_matvec=0):
     import torch
+    from pyprop_gb300 import _native
     dt = torch.complex128 if prob.psi.GetData().dtype == torch.complex128 else torch.complex64
     d = torch.as_tensor(np.ascontiguousarray(psi0)).to("cuda", dt)
-    prob.Propagator.Handle().advance(d, scalings_for(prob, nsteps), prob.TimeStep)
+    h = prob.Propagator.Handle()
+    if round_matvec:
+        h.debug_set(_native.DEBUG_ROUND_MATVEC, round_matvec)
+    try:
+        h.advance(d, scalings_for(prob, nsteps), prob.TimeStep)
+        h.synchronize()
+    finally:
+        if round_matvec:
+            h.debug_set(_native.DEBUG_ROUND_MATVEC, 0)
     return d.cpu().numpy().astype(np.complex128)
 
 
@@ -50,12 +59,21 @@ def test_mixed_vs_fp64(pair, start):
         psi0 = states[0].reshape(p64.psi.GetData().shape)
     want = _run(p64, psi0, 500)
     got = _run(p32, psi0, 500)
+    # the floors: the FP64 path with only its band matvec outputs rounded to complex64 (what the
+    # operator output's storage alone costs), and with every vector of the Arnoldi loop rounded
+    # where the mixed path stores it as complex64 (solve, band and Gram-Schmidt outputs): the
+    # cost of complex64 storage with FP64 arithmetic
+    floor_mv = rel(_run(p64, psi0, 500, round_matvec=1), want)
+    floor = rel(_run(p64, psi0, 500, round_matvec=3), want)
     err = rel(got, want)
     r64, r32 = ob.report(want, states, S), ob.report(got, states, S)
     dpop = float(np.abs(r64["populations"] - r32["populations"]).max())
     dion = abs(r64["ionisation"] - r32["ionisation"])
-    print("\n%s start, 500 steps: rel L2 %.3e | max |d population| %.3e | d ionisation %.3e | "
-          "ionisation fp64 %.6f" % (start, err, dpop, dion, r64["ionisation"]))
+    print("\n%s start, 500 steps: rel L2 %.3e (complex64 floors: matvec outputs %.3e, all Arnoldi vectors %.3e) | "
+          "max |d population| %.3e | d ionisation %.3e | ionisation fp64 %.6f"
+          % (start, err, floor_mv, floor, dpop, dion, r64["ionisation"]))
+    # the mixed arithmetic adds little to what complex64 storage costs
+    assert err <= 2.0 * floor
     if start == "ground":
         # a physical start: every complex64 rounding enters as noise on a smooth state
         assert err <= 1e-6
@@ -63,5 +81,4 @@ def test_mixed_vs_fp64(pair, start):
     else:
         # random B-spline coefficients put most of the norm in the highest modes, where
         # complex64 output rounding (~6e-8 * |H v|) accumulates: bound observables still agree
-        assert err <= 5e-5
         assert dpop <= 1e-7 and dion <= 1e-6

@@ -356,10 +356,23 @@ def test_host_buffer_entry_point(small):
     assert rel(psi, g["psi20"]) < 1e-12
 
 
-def test_mixed_precision_error_report():
-    """FP32-mixed (complex64 basis/matvec/state, FP64 reductions/expm): error vs the FP64 oracle."""
+def test_mixed_precision_error_report(small):
+    """FP32-mixed (complex64 basis and matvec storage, FP32-pair reductions, double-float
+    exponential): error vs the FP64 oracle, bounded by the complex64 storage floor (the FP64
+    path with the outputs of its solves, band matvec and Gram-Schmidt update rounded to
+    complex64) on the same start."""
     import pyprop_gb300 as pp
+    from pyprop_gb300 import _native
     g = np.load(GOLD)
+    h64 = small.Propagator.Handle()
+    d = _torch().as_tensor(np.ascontiguousarray(g["psi0"])).cuda()
+    h64.debug_set(_native.DEBUG_ROUND_MATVEC, 3)
+    try:
+        h64.advance(d, g["scalings"][:500], complex(g["dt"]))
+        h64.synchronize()
+    finally:
+        h64.debug_set(_native.DEBUG_ROUND_MATVEC, 0)
+    floor = rel(d.cpu().numpy(), g["psi500"])
     conf = pp.Load(os.path.join(os.path.dirname(__file__), "..", "pyprop_gb300", "configs",
                                 "hydrogen_velocity_small.ini"))
     conf.Propagation.Set("krylov_precision", "fp32-mixed")
@@ -369,10 +382,10 @@ def test_mixed_precision_error_report():
     for _ in prob.Advance(1):
         pass
     err = rel(prob.psi.GetDataNumpy().astype(np.complex128), g["psi500"])
-    print("500-step FP32-mixed relative L2 vs FP64 oracle: %.3e" % err)
-    # complex64 rounding of the Krylov vectors of this random (high-energy) state: regression
-    # bound; the ground-state case and the observables are in test_gpu_mixed.py
-    assert err < 1e-4
+    print("500-step FP32-mixed relative L2 vs FP64 oracle: %.3e (complex64 storage floor %.3e)" % (err, floor))
+    # complex64 storage of the Krylov vectors of this random (high-energy) state sets the floor;
+    # the ground-state case and the observables are in test_gpu_mixed.py
+    assert err <= 2.0 * floor
 
 
 @pytest.mark.parametrize("prec,n,nv", [(0, 64000, 11), (0, 1060, 1), (1, 5003, 30), (0, 77, 45)])
