@@ -42,9 +42,14 @@ FP32_PEAK_TFLOPS = 69.9
 # capture each comes from is named in PHASE_TRAFFIC_SOURCE)
 PHASE_TRAFFIC = {
     ("fp64", "band"): 20802560, ("fp32-mixed", "band"): 20300288,
+    ("fp64", "solve"): 1408256, ("fp32-mixed", "solve"): 826000,
+    ("fp64", "gram_schmidt"): 16416768,
 }
 PHASE_TRAFFIC_SOURCE = {
-    "band": "profiles/band_kernel_hydrogen_large.md (ncu --set full, one launch)",
+    "band": "profiles/band_kernel_hydrogen_large.md (ncu, dram__bytes_read/write.sum, one launch)",
+    "solve": "profiles/k_solve_inv_fp64_hydrogen_large.md, profiles/k_solve_mixed_hydrogen_large.md "
+             "(ncu --set full, one launch; the inverse band and the factor stay in L2)",
+    "gram_schmidt": "profiles/k_arnoldi_cgs_hydrogen_large.md (ncu --set full, Arnoldi step J = 14)",
 }
 GOLD_LARGE = os.path.join(ROOT, "tests", "golden", "oracle_large.npz")
 
@@ -794,7 +799,8 @@ def measure_single(args, precision, device, world, with_e2e=True):
         "config": {"workload": "hydrogen_velocity_%s" % args.workload, "nl": nl, "nr": nr, "order": 7, "m": m,
                    "dt": dt.real, "precision": precision, "l2": "flushed between steps (%d MB write)" % args.flush_mb,
                    "parallelism": "replicas" if world > 1 else "single", "inverse_band": w,
-                   "band_variant": prob.Propagator.BandVariant, "expm_scaling_order": sorder},
+                   "band_variant": prob.Propagator.BandVariant, "expm_scaling_order": sorder,
+                   "solve_chunks": list(h.tuning()[1])},
         "e2e": e2e,
         "roofline": roofline,
         "step_bytes": {"algorithmic_per_step": B_step, "achieved_GBps": B_step * value / world / 1e9,

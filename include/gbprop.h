@@ -257,6 +257,13 @@ gbprop_status gbprop_expokit_advance(gbprop_handle h, void* psi, int nsteps, con
  * No counterpart in the reference (its generated kernels have one shape). */
 gbprop_status gbprop_autotune(gbprop_handle h, int* variant);
 
+/* The choices gbprop_autotune made (or that were pinned): the band kernel's tile variant and
+ * the radial chunk counts of the two overlap-factor solve directions (U^-1, U^-T; 0 = the
+ * block solver).  The environment GBPROP_BAND_VARIANT=v and GBPROP_SOLVE_CHUNKS=n0,n1 make
+ * gbprop_autotune use those instead of timing them (a profiler run reproduces a live run's
+ * configuration).  No counterpart in the reference. */
+gbprop_status gbprop_get_tuning(gbprop_handle h, int* band_variant, int* solve_chunks);
+
 /* Batches of independent problems (each a finalized handle, all of one precision,
  * each with its own operator, sizes, Krylov size, time function and time step),
  * advanced together: one step of the batch is a single CUDA graph launch whose

@@ -93,6 +93,7 @@ _PROTOS = {
     "gbprop_get_hessenberg": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gbprop_synchronize": (C.c_int, [C.c_void_p]),
     "gbprop_debug_set": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong]),
+    "gbprop_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
     "gbprop_debug_expm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p,
                                     C.POINTER(C.c_int)]),
     "gbprop_time_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
@@ -257,6 +258,14 @@ class Handle:
 
     def reset_stats(self):
         check(lib().gbprop_reset_stats(self._h))
+
+    def tuning(self):
+        """(band-kernel variant, (U^-1 solve chunks, U^-T solve chunks)) chosen by the autotuner."""
+        import numpy as np
+        v = C.c_int()
+        ch = np.zeros(2, dtype=np.int32)
+        check(lib().gbprop_get_tuning(self._h, C.byref(v), ch.ctypes.data))
+        return v.value, (int(ch[0]), int(ch[1]))
 
     def hessenberg(self):
         import numpy as np

@@ -1320,7 +1320,14 @@ gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
     GB_CUDA(cudaMemsetAsync(h->d_s, 0, (size_t)h->N * h->kelem(), s));
     int best = h->band_variant;
     float best_ms = 1e30f;
-    for (int v = 0; v < band_variant_count(); ++v) {
+    // GBPROP_BAND_VARIANT=v and GBPROP_SOLVE_CHUNKS=n0,n1 pin the choices instead of timing them
+    // (a profiler's serialised launches time differently from a live run)
+    const char* env_v = std::getenv("GBPROP_BAND_VARIANT");
+    const int pin_v = env_v ? std::atoi(env_v) : -1;
+    int pin_c[2] = {0, 0};
+    if (const char* env_c = std::getenv("GBPROP_SOLVE_CHUNKS")) std::sscanf(env_c, "%d,%d", &pin_c[0], &pin_c[1]);
+    if (pin_v >= 0 && pin_v < band_variant_count()) best = pin_v;
+    for (int v = 0; v < band_variant_count() && !(pin_v >= 0 && pin_v < band_variant_count()); ++v) {
         h->t64.op.variant = v;
         h->t32.op.variant = v;
         for (int k = 0; k < 3; ++k)
@@ -1342,6 +1349,10 @@ gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
         GB_CUDA(cudaMemsetAsync(h->d_s, 0x3f, (size_t)h->N * h->kelem(), s));
         for (int dir = 0; dir < 2; ++dir) {
             const InvTab keep = h->inv[dir];
+            if (pin_c[dir] > 0) {
+                if (!set_inv_chunk_count(h, dir, pin_c[dir])) h->inv[dir] = keep;
+                continue;
+            }
             InvTab best_t = keep;
             float best_s = 1e30f;
             for (int nch = 1; nch <= 8; ++nch) {
@@ -1363,6 +1374,16 @@ gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
     cudaEventDestroy(e1);
     set_band_variant(h, best);
     if (variant) *variant = best;
+    return GBPROP_OK;
+}
+
+gbprop_status gbprop_get_tuning(gbprop_handle h, int* band_variant, int* solve_chunks) {
+    if (gbprop_status st = check_handle(h, true)) return st;
+    if (band_variant) *band_variant = h->band_variant;
+    if (solve_chunks) {
+        solve_chunks[0] = h->inv_ok ? h->inv[0].nchunks : 0;
+        solve_chunks[1] = h->inv_ok ? h->inv[1].nchunks : 0;
+    }
     return GBPROP_OK;
 }
 
