@@ -714,9 +714,11 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
         }
         GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, v0s, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 0,
                                  dorth, s));
+        // without re-orthogonalisation the update's last block also finalizes the step
+        const bool fin = !dorth && J < m - 1;
         if (J < m - 1 || dorth)
             GB_LAUNCH(launch_cgs_update(kp, V, h->d_v0, v0s, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl,
-                                        dorth ? 2 : 0, s));
+                                        dorth ? 2 : (fin ? 4 : 0), s, h->d_H, m, brk_tol));
         if (dorth) {
             for (int pass = 0; pass < 3; ++pass) {
                 GB_LAUNCH(launch_cgs_dot(kp, V, h->d_v0, v0s, N, J + 1, h->d_r, h->d_partials, h->d_counter, h->d_ctrl, 1, 0,
@@ -725,7 +727,7 @@ gbprop_status enqueue_arnoldi(gbprop_ctx* h, int dorth, double brk_tol) {
                                             s));
             }
         }
-        GB_LAUNCH(launch_arnoldi_finalize(h->d_ctrl, h->d_H, m, J, dorth, brk_tol, s));
+        if (!fin) GB_LAUNCH(launch_arnoldi_finalize(h->d_ctrl, h->d_H, m, J, dorth, brk_tol, s));
         tick(h, GBPROP_PHASE_GRAM_SCHMIDT);
     }
     return GBPROP_OK;

@@ -215,8 +215,12 @@ cudaError_t launch_cgs_dot(int prec, const void* V, const double2* v0, const flo
 size_t block_inner_scratch_doubles(long n, int nvals);
 cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const void* w, int want_norm, double* out,
                                double* partials, unsigned* counter, cudaStream_t s);
+// mode: bit 0 re-orthogonalisation pass, bit 1 double orthogonalisation requested, bit 2 the
+// last block also finalizes Arnoldi step nv - 1 (H column, beta, breakdown; H, m, brk_tol as
+// launch_arnoldi_finalize)
 cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, const float4* v0s, long n, int nv, void* w,
-                              double* partials, unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s);
+                              double* partials, unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s,
+                              double* H = nullptr, int m = 0, double brk_tol = 0.0);
 // brk_tol: happy-breakdown threshold on the new basis norm (pAMP: sqrt(eps), pamp.h:79;
 // Expokit: 1e-7).
 cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol,

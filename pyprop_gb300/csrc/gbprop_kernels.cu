@@ -789,12 +789,18 @@ cudaError_t launch_block_inner(int prec, const void* V, long n, int nv, const vo
 // The basis loads of four vectors are issued together per step of the k loop.
 constexpr int kUpdThreads = 256;
 
+__device__ void arnoldi_finalize_block(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol);
+
+// mode bit 2 (primary pass without re-orthogonalisation): the last block also writes the
+// Hessenberg column J, the next beta and the breakdown decision (k_arnoldi_finalize), one
+// launch fewer per Arnoldi step.
 template <typename T>
 __global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restrict__ V,
                                                             const double2* __restrict__ v0,
                                                             const float4* __restrict__ v0s, long n, int nv,
                                                             cx<T>* __restrict__ w, double* partials,
-                                                            unsigned* counter, Ctrl* ctrl, int mode) {
+                                                            unsigned* counter, Ctrl* ctrl, int mode, double* H,
+                                                            int m, double brk_tol) {
     using C = cx<T>;
     __shared__ C hs[kMaxBasis];
     __shared__ C hl[kMaxBasis];
@@ -913,27 +919,31 @@ __global__ void __launch_bounds__(kUpdThreads) k_cgs_update(const cx<T>* __restr
             __syncthreads();
             for (int k = threadIdx.x; k < 2 * nv; k += blockDim.x) ctrl->h[k] += ctrl->h3[k];
         }
+        if (mode & 4) {
+            __syncthreads();
+            arnoldi_finalize_block(ctrl, H, m, nv - 1, 0, brk_tol);
+        }
     }
 }
 
 cudaError_t launch_cgs_update(int prec, const void* V, const double2* v0, const float4* v0s, long n, int nv, void* w,
-                              double* partials, unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s) {
+                              double* partials, unsigned* counter, Ctrl* ctrl, int mode, cudaStream_t s, double* H,
+                              int m, double brk_tol) {
     count_launch();
     int blocks = (int)((n + kUpdThreads - 1) / kUpdThreads);
     if (blocks > grid_reduce_blocks() * 4) blocks = grid_reduce_blocks() * 4;
     if (prec == 0)
         k_cgs_update<double><<<blocks, kUpdThreads, 0, s>>>((const double2*)V, nullptr, nullptr, n, nv, (double2*)w,
-                                                            partials, counter, ctrl, mode);
+                                                            partials, counter, ctrl, mode, H, m, brk_tol);
     else
         k_cgs_update<float><<<blocks, kUpdThreads, 0, s>>>((const float2*)V, v0, v0s, n, nv, (float2*)w, partials,
-                                                           counter, ctrl, mode);
+                                                           counter, ctrl, mode, H, m, brk_tol);
     return cudaGetLastError();
 }
 
 // Writes Hessenberg column J, the next beta and the happy-breakdown decision
-// (pamp.h:305-315, 345).
-__global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol) {
-    if (ctrl->broken) return;
+// (pamp.h:305-315, 345).  One block (its threads share the column).
+__device__ void arnoldi_finalize_block(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol) {
     const int nv = J + 1;
     for (int k = threadIdx.x; k < nv; k += blockDim.x) {
         H[2 * ((size_t)k * m + J)] = ctrl->h[2 * k];
@@ -959,6 +969,11 @@ __global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int doub
             }
         }
     }
+}
+
+__global__ void k_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol) {
+    if (ctrl->broken) return;
+    arnoldi_finalize_block(ctrl, H, m, J, double_orth, brk_tol);
 }
 
 cudaError_t launch_arnoldi_finalize(Ctrl* ctrl, double* H, int m, int J, int double_orth, double brk_tol,
