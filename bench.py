@@ -140,6 +140,21 @@ def algorithmic_bytes(N, m, s, coef_bytes):
     return 2 * N * s + coef_bytes, s * N * (m * m + 7 * m + 3) + m * coef_bytes
 
 
+def fp64_ops_per_step(N, nr, m, kd, nterms, kb):
+    """Algorithmic FP64 FMA-pipe operations (thread instructions) of one FP64 Krylov step: band
+    matvec (2 per real coefficient and complex element, 4 per term factor and element), classical
+    Gram-Schmidt (4 per complex product in the dots and in the update, 2 per element of each norm),
+    the last refinement residual of the 2m overlap-factor solves (2 per band entry and 2 adds per
+    element), and the combination (4 per basis vector and element).  The exponential (m^3 per
+    product) is below 1%."""
+    W = 2 * kb + 1
+    band = m * nterms * nr * (2 * W + 4)
+    gs = N * (4 * m * (m + 1) + 2 * m)
+    solves = 2 * m * N * (2 * (kd + 1) + 2)
+    combine = 4 * m * N
+    return band + gs + solves + combine
+
+
 def operator_slots(prob):
     """(band slots, terms) of the device operator: one real band per stored angular
     slot and non-zero part (real / imaginary) of each consolidated TensorPotential."""
@@ -809,6 +824,14 @@ def measure_single(args, precision, device, world, with_e2e=True):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    if precision == "fp64":
+        # the FP64 step's own bound: FP64 FMA-pipe operations per step against the measured issue rate
+        ops = fp64_ops_per_step(N, nr, m, kd, nterms, kd)
+        line["step_fp64_roofline"] = {
+            "fp64_ops_per_step": ops, "unit": "TFLOP/s (2 per FMA-pipe operation)",
+            "achieved": 2 * ops * value / world / 1e12, "peak": FP64_PEAK_TFLOPS,
+            "peak_source": "measured FP64 FMA issue rate on GB300",
+            "frac": 2 * ops * value / world / 1e12 / FP64_PEAK_TFLOPS}
     par = parity_vs_fixture(args.workload, h, precision)
     if par is not None:
         line["parity_vs_oracle"] = par
