@@ -257,6 +257,24 @@ gbprop_status gbprop_expokit_advance(gbprop_handle h, void* psi, int nsteps, con
  * No counterpart in the reference (its generated kernels have one shape). */
 gbprop_status gbprop_autotune(gbprop_handle h, int* variant);
 
+/* Field-free bound states: for every angular row l the eigenpairs with E < emax of the
+ * generalized symmetric banded problem H_l c = E S c (the static angular-diagonal operator of
+ * row l in the B-spline overlap metric) -- the analysis of the reference's hydrogen example
+ * (examples/tensor/helium_stabilization_sae/analysis.py:92-160, a dense generalized
+ * eigensolver per l there).  Here: inertia counts of banded LDL^T factorisations of
+ * H - sigma S, bisection to the double-precision eigenvalue (one GPU thread per state) and
+ * inverse iteration for the vector, normalised in the S metric (sign arbitrary).
+ *   h_bands  DEVICE, nrows x (2kd+1) x nr doubles: h_bands[(l (2kd+1) + d) nr + i] = H_l(i, i+d-kd)
+ *            (symmetric; the lower half and the diagonal are read)
+ *   s_band   DEVICE, (2kd+1) x nr doubles, S(i, i+d-kd), positive definite
+ *   counts   HOST out, nrows: the number of eigenvalues below emax of each row (states beyond
+ *            max_states are not computed)
+ *   energies HOST out, nrows x max_states (unused slots 0)
+ *   vectors  DEVICE out, nrows x max_states x nr (slot (l, k) for k < min(counts[l], max_states))
+ * Synchronises `stream`.  No counterpart in the reference. */
+gbprop_status gbprop_bound_states(int nr, int kd, int nrows, const double* h_bands, const double* s_band, double emax,
+                                  int max_states, int* counts, double* energies, double* vectors, void* stream);
+
 /* The choices gbprop_autotune made (or that were pinned): the band kernel's tile variant and
  * the radial chunk counts of the two overlap-factor solve directions (U^-1, U^-T; 0 = the
  * block solver).  The environment GBPROP_BAND_VARIANT=v and GBPROP_SOLVE_CHUNKS=n0,n1 make

@@ -94,6 +94,8 @@ _PROTOS = {
     "gbprop_synchronize": (C.c_int, [C.c_void_p]),
     "gbprop_debug_set": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong]),
     "gbprop_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
+    "gbprop_bound_states": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gbprop_debug_expm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p,
                                     C.POINTER(C.c_int)]),
     "gbprop_time_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
@@ -401,6 +403,25 @@ def bspline_bands(bspline, terms, cholesky=False, stream=None):
                                      len(terms), ptr(fid), ptr(der), ptr(coef), ptr(out), ptr(ch),
                                      C.c_void_p(stream or 0)))
     return [out[m] for m in range(len(terms))], ch
+
+
+def bound_states(h_bands, s_band, emax=0.0, max_states=64, stream=None):
+    """gbprop_bound_states: h_bands (nrows, 2kd+1, nr) and s_band (2kd+1, nr) float64 CUDA tensors
+    (symmetric bands, diagonal-major).  Returns (counts (nrows,) numpy, energies (nrows,
+    max_states) numpy, vectors (nrows, max_states, nr) float64 CUDA tensor)."""
+    import numpy as np
+    import torch
+    nrows, W, nr = h_bands.shape
+    kd = (W - 1) // 2
+    hb = h_bands.contiguous()
+    sb = s_band.contiguous()
+    counts = np.zeros(nrows, dtype=np.int32)
+    energies = np.zeros((nrows, max_states), dtype=np.float64)
+    vectors = torch.zeros((nrows, max_states, nr), dtype=torch.float64, device=hb.device)
+    st = torch.cuda.current_stream(hb.device).cuda_stream if stream is None else stream
+    check(lib().gbprop_bound_states(nr, kd, nrows, ptr(hb), ptr(sb), float(emax), int(max_states), ptr(counts),
+                                    ptr(energies), ptr(vectors), C.c_void_p(st)))
+    return counts, energies, vectors
 
 
 def launch_count():

@@ -48,11 +48,12 @@ def hat_weights(times, T, nsamples):
     return W
 
 
-def bound_states(problem, emax=0.0, lmax_states=None):
+def bound_states(problem, emax=0.0, lmax_states=None, solver="host"):
     """Bound eigenstates (E < emax) of a batch.HydrogenProblem's field-free Hamiltonian, per l,
-    S-normalised physical coefficient vectors (observables.hydrogen_bound_states)."""
+    S-normalised physical coefficient vectors (observables.hydrogen_bound_states; solver "gpu":
+    the banded GPU eigensolver)."""
     from .observables import hydrogen_bound_states
-    return hydrogen_bound_states(problem, emax, lmax_states)
+    return hydrogen_bound_states(problem, emax, lmax_states, solver=solver)
 
 
 class AugmentedOperator:

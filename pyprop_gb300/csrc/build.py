@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbprop.so")
 SOURCES = ["gbprop_kernels.cu", "gbprop_solve.cu", "gbprop_cgs.cu", "gbprop_expm.cu", "gbprop_api.cpp",
-           "gbprop_noalloc.cu", "gbprop_setup.cu"]
+           "gbprop_noalloc.cu", "gbprop_setup.cu", "gbprop_bound.cu"]
 # per-file flags: the set-up kernels reproduce the host restatement's roundings (no FMA contraction)
 EXTRA = {"gbprop_setup.cu": ["-fmad=false"]}
 HEADERS = ["gbprop_internal.h", "gbprop_device.cuh", os.path.join(ROOT, "include", "gbprop.h")]

@@ -1379,6 +1379,19 @@ gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
     return GBPROP_OK;
 }
 
+gbprop_status gbprop_bound_states(int nr, int kd, int nrows, const double* h_bands, const double* s_band, double emax,
+                                  int max_states, int* counts, double* energies, double* vectors, void* stream) {
+    if (nr < 1 || kd < 1 || kd > 8 || nrows < 1 || max_states < 1)
+        return fail(GBPROP_EINVAL, "bound states: sizes (nr >= 1, 1 <= kd <= 8, nrows >= 1, max_states >= 1)");
+    if (!h_bands || !s_band || !counts || !energies || !vectors) return fail(GBPROP_EINVAL, "null argument");
+    if (!(emax == emax)) return fail(GBPROP_EINVAL, "emax is NaN");
+    int nt = 0;
+    cudaError_t e = launch_bound_states(h_bands, s_band, nr, kd, nrows, emax, max_states, counts, energies, vectors,
+                                        (cudaStream_t)stream, &nt);
+    if (e != cudaSuccess) return fail(GBPROP_ECUDA, std::string("bound states: ") + cudaGetErrorString(e));
+    return GBPROP_OK;
+}
+
 gbprop_status gbprop_get_tuning(gbprop_handle h, int* band_variant, int* solve_chunks) {
     if (gbprop_status st = check_handle(h, true)) return st;
     if (band_variant) *band_variant = h->band_variant;

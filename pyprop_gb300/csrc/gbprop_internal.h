@@ -262,6 +262,10 @@ cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s);
 
 int grid_reduce_blocks();
 int band_variant_count();
+// Bound states of banded generalized symmetric problems (gbprop_bound.cu; see gbprop_bound_states)
+cudaError_t launch_bound_states(const double* Hb, const double* Sb, int n, int kd, int nrows, double emax,
+                                int max_states, int* counts, double* energies, double* vectors, cudaStream_t s,
+                                int* ntasks);
 size_t partials_capacity();
 
 }  // namespace gbprop

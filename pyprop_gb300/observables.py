@@ -46,8 +46,55 @@ def bound_states(nl, nr, kb, S, static_rows, emax=0.0, lmax_states=None):
     return np.array(states), np.array(energies), np.array(ls)
 
 
-def problem_bound_states(problem, emax=0.0, lmax_states=None):
-    """bound_states() of a pyprop_gb300.Problem (its consolidated static Diag potentials)."""
+def _symmetric_bands(v, nr, kb):
+    """Diagonal-major symmetric band B[d, i] = (H(i, i+d-kb) + H(i+d-kb, i)) / 2 of a row's
+    BandNH data (real part; the static operators are real)."""
+    W = 2 * kb + 1
+    v = np.asarray(v).real
+    B = np.zeros((W, nr))
+    for d in range(W):
+        off = d - kb
+        i = np.arange(max(0, -off), min(nr, nr - off))
+        j = i + off
+        B[d, i] = v[j * W + kb + i - j]
+    Bs = np.zeros_like(B)
+    for d in range(W):
+        off = d - kb
+        i = np.arange(max(0, -off), min(nr, nr - off))
+        Bs[d, i] = 0.5 * (B[d, i] + B[2 * kb - d, i + off])
+    return Bs
+
+
+def bound_states_device(nl, nr, kb, Sdiag, static_rows, emax=0.0, lmax_states=None, max_states=64, device="cuda"):
+    """bound_states() on the GPU (gbprop_bound_states: inertia counts of banded LDL^T
+    factorisations, bisection, inverse iteration; one thread per state), from the banded
+    operators directly -- no dense eigenproblem.  Sdiag: overlap diagonals D[kb + d, i] =
+    S(i, i+d).  Same return values as bound_states() (numpy)."""
+    import torch
+
+    from . import _native
+    last = nl if lmax_states is None else min(nl, lmax_states + 1)
+    Sdiag = np.ascontiguousarray(np.asarray(Sdiag, dtype=np.float64))
+    if Sdiag.shape != (2 * kb + 1, nr):
+        raise ValueError("overlap diagonals must be (2kb+1, nr) = %s, got %s" % ((2 * kb + 1, nr), Sdiag.shape))
+    Hb = np.stack([_symmetric_bands(static_rows[l], nr, kb) for l in range(last)])
+    counts, energies, vecs = _native.bound_states(torch.as_tensor(Hb, device=device),
+                                                  torch.as_tensor(Sdiag, device=device), emax, max_states)
+    vecs = vecs.cpu().numpy()
+    states, es, ls = [], [], []
+    for l in range(last):
+        for k in range(min(int(counts[l]), max_states)):
+            phi = np.zeros((nl, nr), dtype=np.complex128)
+            phi[l] = vecs[l, k]
+            states.append(phi.ravel())
+            es.append(energies[l, k])
+            ls.append(l)
+    return np.array(states), np.array(es), np.array(ls)
+
+
+def problem_bound_states(problem, emax=0.0, lmax_states=None, solver="host"):
+    """bound_states() of a pyprop_gb300.Problem (its consolidated static Diag potentials);
+    solver "gpu": bound_states_device()."""
     repr_ = problem.psi.GetRepresentation()
     nl, nr = repr_.GetFullShape()
     rad = repr_.radial
@@ -66,11 +113,15 @@ def problem_bound_states(problem, emax=0.0, lmax_states=None):
         else:
             raise NotImplementedError("bound states need angular-diagonal static potentials (got %s)" % s0)
         static = rows if static is None else static + rows
+    if solver == "gpu":
+        return bound_states_device(nl, nr, kb, rad.overlap_diagonals(), static, emax, lmax_states)
     return bound_states(nl, nr, kb, S, static, emax, lmax_states)
 
 
-def hydrogen_bound_states(hp, emax=0.0, lmax_states=None):
-    """bound_states() of a batch.HydrogenProblem."""
+def hydrogen_bound_states(hp, emax=0.0, lmax_states=None, solver="host"):
+    """bound_states() of a batch.HydrogenProblem; solver "gpu": bound_states_device()."""
+    if solver == "gpu":
+        return bound_states_device(hp.nl, hp.nr, hp.kb, hp.Sdiag, hp.static, emax, lmax_states)
     S = _dense_from_diagonals(hp.Sdiag, hp.kd, hp.nr)
     return bound_states(hp.nl, hp.nr, hp.kb, S, hp.static, emax, lmax_states)
 
