@@ -37,6 +37,11 @@ def test_version_and_errors_without_device():
     assert st == 7
     st = L.gbprop_advance(None, None, 1, None, 0.1, 0.0)
     assert st == 1
+    # the banded bound-state solver validates sizes and pointers before touching a device
+    st = L.gbprop_bound_states(100, 9, 4, None, None, 0.0, 8, None, None, None, None)   # kd > 8
+    assert st == 1 and b"sizes" in L.gbprop_last_error()
+    st = L.gbprop_bound_states(100, 6, 4, None, None, 0.0, 8, None, None, None, None)
+    assert st == 1 and b"null" in L.gbprop_last_error()
 
 
 def test_product_fails_loudly_without_device(small_problem_cpu):
