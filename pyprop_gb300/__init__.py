@@ -7,7 +7,7 @@ step itself runs in libgbprop (CUDA, sm_103a) behind a C ABI (include/gbprop.h).
 from .config import Config, Load, LoadString, Section
 from .initial import GaussianRandomState
 from .potentials import LaserFunctionSimpleLength, LaserFunctionVelocity, PiecewiseLinearField
-from .problem import InitialConditionType, LoadPropagator, Problem
+from .problem import InitialConditionType, LoadPropagator, Problem, WavefunctionFileFormat
 from .propagator import BasisPropagator, ExpokitPropagator, PamPropagator, PropagatorBase
 from .representation import (BSplineRepresentation, CombinedRepresentation, ReducedSphericalHarmonicRepresentation,
                              Wavefunction)
@@ -17,6 +17,6 @@ from .namespace import PotentialType
 __all__ = [
     "Config", "Load", "LoadString", "Section", "Problem", "LoadPropagator", "PamPropagator", "ExpokitPropagator", "BasisPropagator",
     "PropagatorBase", "TensorPotential", "Wavefunction", "CombinedRepresentation", "BSplineRepresentation",
-    "ReducedSphericalHarmonicRepresentation", "InitialConditionType", "PotentialType", "LaserFunctionVelocity",
+    "ReducedSphericalHarmonicRepresentation", "InitialConditionType", "WavefunctionFileFormat", "PotentialType", "LaserFunctionVelocity",
     "LaserFunctionSimpleLength", "PiecewiseLinearField", "GaussianRandomState",
 ]

@@ -46,6 +46,7 @@ def eval_namespace():
     ns["core"] = _core_namespace()
     ns["PotentialType"] = PotentialType
     ns["InitialConditionType"] = problem.InitialConditionType
+    ns["WavefunctionFileFormat"] = problem.WavefunctionFileFormat
     ns["PamPropagator"] = propagator.PamPropagator
     ns["ExpokitPropagator"] = propagator.ExpokitPropagator
     ns["BasisPropagator"] = propagator.BasisPropagator

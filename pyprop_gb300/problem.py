@@ -26,6 +26,13 @@ class InitialConditionType:
     Custom = "Custom"
 
 
+class WavefunctionFileFormat:
+    """File formats of InitialConditionType.File (Enum.py:21-24)."""
+    Ascii = 1
+    Binary = 2
+    HDF = 3
+
+
 def CreateRepresentation(config):
     """CreateRepresentation + CreateSubRepresentations (CreateInstance.py:42-87)."""
     rsec = config.Representation
@@ -194,8 +201,60 @@ class Problem:
             obj = ic.classname()
             ic.Apply(obj)
             obj.SetupWavefunction(self.psi)
+        elif t == InitialConditionType.File:
+            self.SetupWavefunctionFile(self.Config)
         else:
             raise ValueError("Invalid InitialConditionType: %r" % (t,))
+
+    # wavefunction files (Problem.py:397-474): the same grid must be used for saving and loading
+    def SetupWavefunctionFile(self, config):
+        fmt = config.InitialCondition.format
+        filename = config.InitialCondition.filename
+        if fmt == WavefunctionFileFormat.Ascii:
+            self.LoadWavefunctionAscii(filename)
+        elif fmt == WavefunctionFileFormat.Binary:
+            self.LoadWavefunctionPickle(filename)
+        elif fmt == WavefunctionFileFormat.HDF:
+            self.LoadWavefunctionHDF(filename, str(config.InitialCondition.dataset))
+        else:
+            raise ValueError("Invalid file format: %r" % (fmt,))
+
+    def LoadWavefunctionData(self, newdata):
+        newdata = np.asarray(newdata)
+        shape = tuple(self.psi.GetData().shape)
+        if newdata.shape != shape:
+            raise ValueError("Invalid shape on loaded wavefunction, got %s expected %s" % (newdata.shape, shape))
+        self.psi.SetData(newdata)
+
+    def SaveWavefunctionPickle(self, filename):
+        """The data array pickled with protocol 2 (serialization/Pickle.py:4-13)."""
+        import pickle
+        with open(filename, "wb") as f:
+            pickle.dump(np.ascontiguousarray(self.psi.GetDataNumpy()), f, 2)
+
+    def LoadWavefunctionPickle(self, filename):
+        """serialization/Pickle.py:15-27; latin-1 decoding also reads arrays pickled by Python 2."""
+        import pickle
+        with open(filename, "rb") as f:
+            arr = pickle.load(f, encoding="latin1")
+        self.LoadWavefunctionData(arr)
+
+    def SaveWavefunctionAscii(self, filename):
+        """Two columns, real and imaginary part (Problem.py:457-460), of the C-ordered data (the
+        reference writes rank-1 data only)."""
+        d = self.psi.GetDataNumpy().ravel()
+        np.savetxt(filename, np.column_stack((d.real, d.imag)), delimiter=" ")
+
+    def LoadWavefunctionAscii(self, filename):
+        r, c = np.loadtxt(filename, unpack=True, ndmin=2)
+        self.LoadWavefunctionData((r + 1j * c).reshape(tuple(self.psi.GetData().shape)))
+
+    def LoadWavefunctionHDF(self, filename, datasetPath):
+        raise NotImplementedError("HDF5 wavefunction files (serialization/WavefunctionHDF.py) need pytables or "
+                                  "h5py; use WavefunctionFileFormat.Binary or Ascii")
+
+    def SaveWavefunctionHDF(self, filename, datasetPath):
+        self.LoadWavefunctionHDF(filename, datasetPath)
 
     def SetupWavefunctionFunction(self, config):
         """f(conf, [l, r]) on (l, radial quadrature points), projected onto the
