@@ -14,6 +14,7 @@
 #include "gbprop_internal.h"
 #include "gbprop_device.cuh"
 
+#include <algorithm>
 #include <cfloat>
 
 namespace gbprop {
@@ -527,6 +528,42 @@ int arnoldi_cgs_grid(int prec, long n, int m, int with_v0, int cache) {
     cudaGetLastError();
     if (e != cudaSuccess || per_sm < 1) return 0;
     return sms;
+}
+
+// Grid of the cooperative form for a problem inside a batch, where other problems fill the
+// GPU: the fewest CTAs whose chunk of V fits in shared memory (V read once per Arnoldi step),
+// else one CTA per ~2048 elements without the cache; 0 when neither is co-resident.
+int arnoldi_cgs_grid_batch(int prec, long n, int m, int with_v0, int* cache) {
+    int dev = 0, sms = 0, coop = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (!coop || sms <= 0) return 0;
+    for (int c = 1; c >= 0; --c) {
+        int grid = c ? 1 : (int)std::min<long>(sms, std::max<long>(1, (n + 2047) / 2048));
+        if (c)
+            while (grid <= sms && arnoldi_cgs_smem(prec, n, m, grid, with_v0, 1) + 4096 > (size_t)optin) ++grid;
+        if (grid > sms) continue;
+        const size_t smem = arnoldi_cgs_smem(prec, n, m, grid, with_v0, c);
+        if (smem + 4096 > (size_t)optin) continue;
+        int per_sm = 0;
+        cudaError_t e;
+        if (prec == 0) {
+            auto kern = c ? k_arnoldi_cgs<true> : k_arnoldi_cgs<false>;
+            allow_max_smem(kern);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFuseThreads, smem);
+        } else {
+            auto kern = c ? k_arnoldi_cgs32<true> : k_arnoldi_cgs32<false>;
+            allow_max_smem(kern);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFuseThreads, smem);
+        }
+        cudaGetLastError();
+        if (e != cudaSuccess || per_sm < 1 || grid > per_sm * sms) continue;
+        *cache = c;
+        return grid;
+    }
+    return 0;
 }
 
 }  // namespace gbprop

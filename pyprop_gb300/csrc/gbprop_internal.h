@@ -237,6 +237,7 @@ cudaError_t launch_arnoldi_cgs(int prec, const void* V, const void* v0, long n, 
                                cudaStream_t s);
 // Grid size for the cooperative Gram-Schmidt (0 if it cannot run co-resident).
 int arnoldi_cgs_grid(int prec, long n, int m, int with_v0, int cache);
+int arnoldi_cgs_grid_batch(int prec, long n, int m, int with_v0, int* cache);
 inline size_t arnoldi_cgs_part_doubles(int grid) { return (size_t)(2 * (kMaxBasis + 1) + 1) * grid; }
 cudaError_t launch_step_begin(Ctrl* ctrl, double* H, int m, cudaStream_t s);
 // max_cluster: 16 lets one problem's exponential spread over a thread-block cluster; 1 keeps it on
