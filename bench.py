@@ -43,13 +43,14 @@ FP32_PEAK_TFLOPS = 69.9
 PHASE_TRAFFIC = {
     ("fp64", "band"): 20802560, ("fp32-mixed", "band"): 20300288,
     ("fp64", "solve"): 1408256, ("fp32-mixed", "solve"): 826000,
-    ("fp64", "gram_schmidt"): 16416768,
+    ("fp64", "gram_schmidt"): 16416768, ("fp32-mixed", "gram_schmidt"): 8750336,
 }
 PHASE_TRAFFIC_SOURCE = {
     "band": "profiles/band_kernel_hydrogen_large.md (ncu, dram__bytes_read/write.sum, one launch)",
     "solve": "profiles/k_solve_inv_fp64_hydrogen_large.md, profiles/k_solve_mixed_hydrogen_large.md "
              "(ncu --set full, one launch; the inverse band and the factor stay in L2)",
-    "gram_schmidt": "profiles/k_arnoldi_cgs_hydrogen_large.md (ncu --set full, Arnoldi step J = 14)",
+    "gram_schmidt": "profiles/k_arnoldi_cgs_hydrogen_large.md, profiles/k_arnoldi_cgs32_hydrogen_large.md "
+                    "(ncu --set full, Arnoldi step J = 14)",
 }
 GOLD_LARGE = os.path.join(ROOT, "tests", "golden", "oracle_large.npz")
 
