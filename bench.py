@@ -922,7 +922,7 @@ def precision_report(device, nsteps=500):
         pr.SetupStep()
         probs[prec] = pr
     p64 = probs["fp64"]
-    states, _, _ = ob.problem_bound_states(p64, solver="gpu")     # banded GPU eigensolver
+    states, _, _ = ob.problem_bound_states(p64)     # banded GPU eigensolver
     S = ob.radial_overlap(p64)
     bp = p64.Propagator.BasePropagator
     times, t = [], p64.PropagatedTime

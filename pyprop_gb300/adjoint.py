@@ -48,10 +48,10 @@ def hat_weights(times, T, nsamples):
     return W
 
 
-def bound_states(problem, emax=0.0, lmax_states=None, solver="host"):
+def bound_states(problem, emax=0.0, lmax_states=None, solver="auto"):
     """Bound eigenstates (E < emax) of a batch.HydrogenProblem's field-free Hamiltonian, per l,
-    S-normalised physical coefficient vectors (observables.hydrogen_bound_states; solver "gpu":
-    the banded GPU eigensolver)."""
+    S-normalised physical coefficient vectors (observables.hydrogen_bound_states; solver "gpu" or
+    "auto" with a CUDA device: the banded GPU eigensolver)."""
     from .observables import hydrogen_bound_states
     return hydrogen_bound_states(problem, emax, lmax_states, solver=solver)
 

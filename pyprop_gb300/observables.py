@@ -92,9 +92,21 @@ def bound_states_device(nl, nr, kb, Sdiag, static_rows, emax=0.0, lmax_states=No
     return np.array(states), np.array(es), np.array(ls)
 
 
-def problem_bound_states(problem, emax=0.0, lmax_states=None, solver="host"):
+def _solver(solver):
+    """"auto": the GPU eigensolver when a CUDA device is present, else the host's."""
+    if solver != "auto":
+        return solver
+    try:
+        import torch
+        return "gpu" if torch.cuda.is_available() else "host"
+    except ImportError:
+        return "host"
+
+
+def problem_bound_states(problem, emax=0.0, lmax_states=None, solver="auto"):
     """bound_states() of a pyprop_gb300.Problem (its consolidated static Diag potentials);
-    solver "gpu": bound_states_device()."""
+    solver "gpu": bound_states_device(), "host": scipy per row, "auto": the GPU when present."""
+    solver = _solver(solver)
     repr_ = problem.psi.GetRepresentation()
     nl, nr = repr_.GetFullShape()
     rad = repr_.radial
@@ -118,9 +130,9 @@ def problem_bound_states(problem, emax=0.0, lmax_states=None, solver="host"):
     return bound_states(nl, nr, kb, S, static, emax, lmax_states)
 
 
-def hydrogen_bound_states(hp, emax=0.0, lmax_states=None, solver="host"):
-    """bound_states() of a batch.HydrogenProblem; solver "gpu": bound_states_device()."""
-    if solver == "gpu":
+def hydrogen_bound_states(hp, emax=0.0, lmax_states=None, solver="auto"):
+    """bound_states() of a batch.HydrogenProblem; solver as problem_bound_states()."""
+    if _solver(solver) == "gpu":
         return bound_states_device(hp.nl, hp.nr, hp.kb, hp.Sdiag, hp.static, emax, lmax_states)
     S = _dense_from_diagonals(hp.Sdiag, hp.kd, hp.nr)
     return bound_states(hp.nl, hp.nr, hp.kb, S, hp.static, emax, lmax_states)

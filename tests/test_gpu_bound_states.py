@@ -27,7 +27,7 @@ def test_bound_states_small_workload_vs_host():
     from pyprop_gb300 import observables as ob
     from helpers import make_problem
     prob = make_problem(maxl=9, xsize=103, m=20, dt=0.01)
-    host = ob.problem_bound_states(prob)
+    host = ob.problem_bound_states(prob, solver="host")
     gpu = ob.problem_bound_states(prob, solver="gpu")
     S = ob.radial_overlap(prob)
     err = _compare(host, gpu, S, S.shape[0])
@@ -38,7 +38,7 @@ def test_bound_states_hydrogen_problem_vs_host_and_hydrogenic_levels():
     from pyprop_gb300 import observables as ob
     from pyprop_gb300.batch import HydrogenProblem
     hp = HydrogenProblem(lmax=12, nr=300, rmax=150.0, m=16, dt=0.01, seed=5)
-    host = ob.hydrogen_bound_states(hp)
+    host = ob.hydrogen_bound_states(hp, solver="host")
     gpu = ob.hydrogen_bound_states(hp, solver="gpu")
     from pyprop_gb300.observables import _dense_from_diagonals
     S = _dense_from_diagonals(hp.Sdiag, hp.kd, hp.nr)
