@@ -428,8 +428,9 @@ def host_cpu():
             "nproc": os.cpu_count()}
 
 
-def run_batch(args, rank, world, local):
-    """256 seeded uneven hydrogen-like problems advanced together (one graph launch per batch step)."""
+def run_batch(args, rank, world, local, emit=True):
+    """256 seeded uneven hydrogen-like problems advanced together (one graph launch per batch step).
+    Prints the line (rank 0) when `emit`, and returns it."""
     import torch
     from pyprop_gb300 import _native
     from pyprop_gb300.batch import BatchPropagator, gather_states, random_batch, shard
@@ -504,8 +505,28 @@ def run_batch(args, rank, world, local):
         v, desc, threads = oracle_batch_rate(full, budget_s=12.0)
         line["cpu_baseline"] = {"value": v, "unit": "batch steps/s", "cores": threads, "kind": "port",
                                 "sample": desc}
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line), flush=True)
+    del bp
+    torch.cuda.synchronize()
+    return line
+
+
+def batch_summary(args, rank, world, local):
+    """The 256-problem batch in both precisions, a few timed steps each, for the default line
+    (the full measurement is --workload batch)."""
+    import copy
+    out = {}
+    for prec in ("fp64", "fp32-mixed"):
+        a = copy.copy(args)
+        a.precision, a.steps, a.warmup, a.no_cpu_baseline = prec, 5, 3, True
+        b = run_batch(a, rank, world, local, emit=False)
+        out[prec] = {k: b[k] for k in ("value", "unit", "ms_per_step", "problem_steps_per_s", "e2e", "gpu_launches")}
+        out[prec]["setup_s"] = b["config"]["setup_s"]
+    out["fp32_mixed_speedup_vs_fp64"] = out["fp32-mixed"]["value"] / out["fp64"]["value"]
+    out["config"] = {"workload": "hydrogen_velocity_batch", "problems": args.batch_size, "steps": 5, "warmup": 3,
+                     "l2": "flushed between steps (%d MB write)" % args.flush_mb}
+    return out
 
 
 def run_adjoint(args, rank, world, local):
@@ -638,6 +659,7 @@ def main():
     ap.add_argument("--flush-mb", type=int, default=512)
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed arm of the default run")
     ap.add_argument("--no-precision-report", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batch summary of the default run")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 20 if args.workload == "batch" else 200
@@ -672,6 +694,8 @@ def main():
         line["fp32_mixed"]["dtype"] = mixed["dtype"]
     if not args.no_precision_report:
         line["precision_report"] = precision_report(device)
+    if world == 1 and not args.no_batch:
+        line["batch"] = batch_summary(args, rank, world, local)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.workload)
     if rank == 0:
