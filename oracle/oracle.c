@@ -2,7 +2,7 @@
  * oracle.c -- CPU restatement of pyprop's pAMP x TensorPotential propagation step.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (pyprop_gb300/, libgbprop)
- * links, loads or calls this file.  It is the checker the GPU kernels are
+ * links, loads or calls this file.  It is the oracle the GPU kernels are
  * compared against (tests/, __graft_entry__.smoke) and the timed CPU baseline
  * of bench.py.  Everything is complex128 arithmetic written out in real and
  * imaginary parts, in the reference's own order of operations where that

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle.c) -- TEST INFRASTRUCTURE ONLY.
 
 Used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the
-checker of the GPU path.  Never imported by pyprop_gb300.
+oracle of the GPU path.  Never imported by pyprop_gb300.
 
 Parity status: the reference cannot be built or run here, so this CPU
 restatement is pinned by the reference's own known-answer check (TestPade,

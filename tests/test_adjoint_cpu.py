@@ -1,5 +1,5 @@
-"""CPU checks of the gradient machinery: the dense discrete adjoint (the checker of
-the GPU adjoint) against finite differences, the augmented block operator against
+"""CPU checks of the gradient machinery: the dense discrete adjoint (the reference
+result for the GPU adjoint) against finite differences, the augmented block operator against
 scipy's Frechet derivative through the CPU oracle, the field-sample weights and the
 bound states used as the observable."""
 import numpy as np
