@@ -1309,10 +1309,18 @@ gbprop_status gbprop_tensor_multiply_bandnh(int storage, const void* V, int npai
     return GBPROP_OK;
 }
 
+// Variants 6 and 7 (two elements per thread, vector loads) need an even radial size.
+bool band_variant_available(const gbprop_ctx* h, int v) {
+    if (v < 0 || v >= band_variant_count()) return false;
+    if (v < 6) return true;
+    if (!band_variant_vec_ok(v, h->nr)) return false;
+    return h->kprec() == 0 || h->t32.op.slots_lo != nullptr;
+}
+
 gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
     if (gbprop_status st = check_handle(h, true)) return st;
     if (variant && *variant >= 0) {                  // explicit choice, no timing
-        if (*variant >= band_variant_count()) return fail(GBPROP_EINVAL, "no such band-kernel variant");
+        if (!band_variant_available(h, *variant)) return fail(GBPROP_EINVAL, "no such band-kernel variant");
         set_band_variant(h, *variant);
         return GBPROP_OK;
     }
@@ -1330,8 +1338,10 @@ gbprop_status gbprop_autotune(gbprop_handle h, int* variant) {
     const int pin_v = env_v ? std::atoi(env_v) : -1;
     int pin_c[2] = {0, 0};
     if (const char* env_c = std::getenv("GBPROP_SOLVE_CHUNKS")) std::sscanf(env_c, "%d,%d", &pin_c[0], &pin_c[1]);
-    if (pin_v >= 0 && pin_v < band_variant_count()) best = pin_v;
-    for (int v = 0; v < band_variant_count() && !(pin_v >= 0 && pin_v < band_variant_count()); ++v) {
+    const bool pinned = band_variant_available(h, pin_v);
+    if (pinned) best = pin_v;
+    for (int v = 0; v < band_variant_count() && !pinned; ++v) {
+        if (!band_variant_available(h, v)) continue;
         h->t64.op.variant = v;
         h->t32.op.variant = v;
         for (int k = 0; k < 3; ++k)
