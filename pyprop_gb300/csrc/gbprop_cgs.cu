@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double hs[2 * (kMaxBasis + 1)];
     __shared__ double red[kFuseThreads / 32];
+    pdl_wait();
     if (ctrl->broken) return;                        // uniform: written only between launches
     const bool rnd = ctrl->round_matvec & 2;        // precision probe (FP64 handles)
     const int nv = J + 1, G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -251,7 +252,6 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
     __shared__ double hs[2 * (kMaxBasis + 1)];
     __shared__ float2 red[kCgsWarps];
     __shared__ __align__(8) unsigned long long s_bar;
-    if (ctrl->broken) return;                        // uniform: written only between launches
     const int nv = J + 1, G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long i0 = (long)b * chunk;
     const int cl = (int)max(0L, min((long)chunk, n - i0));
@@ -264,6 +264,11 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
     // is a multiple of 8).
     const bool tma = CACHE && (n & 1) == 0 && cl > 0;
     const int k_first = v0s ? 1 : 0;                 // rows of V read (row 0 replaced by v0s)
+    // The basis rows and the split first vector were written by kernels before the
+    // predecessor, so their copies are issued before the dependency wait (overlapping the
+    // predecessor's tail); w, the predecessor's output, and the control block after it.  The
+    // barrier's single arrival comes with w's bytes, so the phase cannot complete early.
+    const unsigned row = (unsigned)cl * 8;
     if (tma) {
         if (tid == 0) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&s_bar)) : "memory");
@@ -271,13 +276,27 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs32(const float2* __
         }
         __syncthreads();
         if (tid == 0) {
-            const unsigned row = (unsigned)cl * 8;
-            const unsigned bytes = row * (unsigned)(1 + (v0s ? 2 : 0) + (nv - k_first));
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                         :: "r"(smem_u32(&s_bar)), "r"(bytes) : "memory");
-            bulk_g2s(ws, w + i0, row, &s_bar);
+            const unsigned bytes = row * (unsigned)((v0s ? 2 : 0) + (nv - k_first));
+            if (bytes)
+                asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;"
+                             :: "r"(smem_u32(&s_bar)), "r"(bytes) : "memory");
             if (v0s) bulk_g2s(c0, v0s + i0, 2 * row, &s_bar);
             for (int k = k_first; k < nv; ++k) bulk_g2s(cache + (size_t)k * chunk, V + (size_t)k * n + i0, row, &s_bar);
+        }
+    }
+    pdl_wait();
+    if (ctrl->broken) {                              // uniform: written only between launches
+        if (tma) {
+            if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(&s_bar)) : "memory");
+            mbar_wait0(&s_bar);                      // copies in flight land before exit
+        }
+        return;
+    }
+    if (tma) {
+        if (tid == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         :: "r"(smem_u32(&s_bar)), "r"(row) : "memory");
+            bulk_g2s(ws, w + i0, row, &s_bar);
         }
         if (!__syncthreads_and(mbar_wait0(&s_bar, wait_budget(ctrl, kInvWaitLimit)))) {
             if (tid == 0) ctrl->wait_timeout = 1;
@@ -479,11 +498,13 @@ static cudaError_t cgs_coop_launch(Kern kern, int grid, size_t smem, cudaStream_
     cfg.blockDim = dim3(kFuseThreads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;   // the kernels call pdl_wait
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = pdl_enabled() ? 2 : 1;
     return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
