@@ -98,17 +98,55 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double hs[2 * (kMaxBasis + 1)];
     __shared__ double red[kFuseThreads / 32];
-    pdl_wait();
-    if (ctrl->broken) return;                        // uniform: written only between launches
-    const bool rnd = ctrl->round_matvec & 2;        // precision probe (FP64 handles)
+    __shared__ __align__(8) unsigned long long s_bar;
     const int nv = J + 1, G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long i0 = (long)b * chunk;
     const int cl = (int)max(0L, min((long)chunk, n - i0));
     // shared memory: w chunk | cached rows of V
     C* ws = reinterpret_cast<C*>(smem_raw);
     C* cache = reinterpret_cast<C*>(smem_raw + (((size_t)chunk * sizeof(C) + 15) & ~(size_t)15));
-    for (int i = tid; i < cl; i += kFuseThreads) ws[i] = w[i0 + i];
-    __syncthreads();
+    // With the cache, the CTA's basis rows (written by kernels before the predecessor) are
+    // copied in by bulk asynchronous copies issued before the dependency wait; w, the
+    // predecessor's output, follows it and carries the barrier's one arrival (rows start on
+    // 16-byte boundaries: 16-byte elements)
+    const bool tma = CACHE && cl > 0;
+    const unsigned row = (unsigned)cl * 16;
+    if (tma) {
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&s_bar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;"
+                         :: "r"(smem_u32(&s_bar)), "r"(row * (unsigned)nv) : "memory");
+            for (int k = 0; k < nv; ++k) bulk_g2s(cache + (size_t)k * chunk, V + (size_t)k * n + i0, row, &s_bar);
+        }
+    }
+    pdl_wait();
+    if (ctrl->broken) {                              // uniform: written only between launches
+        if (tma) {
+            if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(&s_bar)) : "memory");
+            mbar_wait0(&s_bar);                      // copies in flight land before exit
+        }
+        return;
+    }
+    const bool rnd = ctrl->round_matvec & 2;        // precision probe (FP64 handles)
+    if (tma) {
+        if (tid == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         :: "r"(smem_u32(&s_bar)), "r"(row) : "memory");
+            bulk_g2s(ws, w + i0, row, &s_bar);
+        }
+        if (!__syncthreads_and(mbar_wait0(&s_bar, wait_budget(ctrl, kInvWaitLimit)))) {
+            if (tid == 0) ctrl->wait_timeout = 1;
+            mbar_wait0(&s_bar);                      // copies in flight land before exit
+            return;
+        }
+    } else {
+        for (int i = tid; i < cl; i += kFuseThreads) ws[i] = w[i0 + i];
+        __syncthreads();
+    }
 
     // ---- phase A: partial inner products, one warp per basis vector.  The FP64 pipe retires
     // one warp instruction per 16 SM cycles and its dependent latency is about as long, so two
@@ -117,31 +155,26 @@ __global__ void __launch_bounds__(kFuseThreads) k_arnoldi_cgs(const double2* __r
         double ar = 0.0, ai = 0.0, br = 0.0, bi = 0.0;
         const C* vk = V + (size_t)k * n + i0;
         int i = lane;
+        const C* ck = cache + (size_t)k * chunk;     // (staged rows when CACHE)
         for (; i + 96 < cl; i += 128) {
             C v[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = vk[i + 32 * u];
+            for (int u = 0; u < 4; ++u) v[u] = CACHE ? ck[i + 32 * u] : vk[i + 32 * u];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                if (CACHE) cache[(size_t)k * chunk + i + 32 * u] = v[u];
                 const C x = ws[i + 32 * u];
                 if (u & 1) acc_dot64(br, bi, v[u].x, v[u].y, x.x, x.y);
                 else acc_dot64(ar, ai, v[u].x, v[u].y, x.x, x.y);
             }
         }
         for (; i + 32 < cl; i += 64) {
-            const C v = vk[i], u = vk[i + 32];
-            if (CACHE) {
-                cache[(size_t)k * chunk + i] = v;
-                cache[(size_t)k * chunk + i + 32] = u;
-            }
+            const C v = CACHE ? ck[i] : vk[i], u = CACHE ? ck[i + 32] : vk[i + 32];
             const C x = ws[i], y = ws[i + 32];
             acc_dot64(ar, ai, v.x, v.y, x.x, x.y);
             acc_dot64(br, bi, u.x, u.y, y.x, y.y);
         }
         if (i < cl) {
-            const C v = vk[i];
-            if (CACHE) cache[(size_t)k * chunk + i] = v;
+            const C v = CACHE ? ck[i] : vk[i];
             const C x = ws[i];
             acc_dot64(ar, ai, v.x, v.y, x.x, x.y);
         }
