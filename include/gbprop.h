@@ -254,7 +254,7 @@ gbprop_status gbprop_expokit_advance(gbprop_handle h, void* psi, int nsteps, con
  * kernel on this handle's operator and keeps the fastest; *variant (if not NULL)
  * receives its index.  Synchronises the handle's stream.  If *variant >= 0 on entry,
  * that shape is selected without timing (GBPROP_EINVAL if it does not exist, or if it
- * does not apply: shapes 6 and 7 form two radial elements per thread and need an even
+ * does not apply: shapes 6, 7 and 8 form two radial elements per thread and need an even
  * radial size).  No counterpart in the reference (its generated kernels have one shape). */
 gbprop_status gbprop_autotune(gbprop_handle h, int* variant);
 

@@ -1309,7 +1309,7 @@ gbprop_status gbprop_tensor_multiply_bandnh(int storage, const void* V, int npai
     return GBPROP_OK;
 }
 
-// Variants 6 and 7 (two elements per thread, vector loads) need an even radial size.
+// Variants 6, 7 and 8 (two elements per thread, vector loads) need an even radial size.
 bool band_variant_available(const gbprop_ctx* h, int v) {
     if (v < 0 || v >= band_variant_count()) return false;
     if (v < 6) return true;

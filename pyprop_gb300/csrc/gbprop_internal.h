@@ -263,7 +263,7 @@ cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s);
 
 int grid_reduce_blocks();
 int band_variant_count();
-bool band_variant_vec_ok(int v, int nr);    // the variant's radial-size condition (even nr for 6, 7)
+bool band_variant_vec_ok(int v, int nr);    // the variant's radial-size condition (even nr for 6, 7, 8)
 // Bound states of banded generalized symmetric problems (gbprop_bound.cu; see gbprop_bound_states)
 cudaError_t launch_bound_states(const double* Hb, const double* Sb, int n, int kd, int nrows, double emax,
                                 int max_states, int* counts, double* energies, double* vectors, cudaStream_t s,

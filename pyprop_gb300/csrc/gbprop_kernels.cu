@@ -152,9 +152,9 @@ __device__ void block_partials<16>(double (&acc)[16], int nvalid, double* partia
 // Tile shapes of the band kernel the autotuner chooses between:
 // (threads per block, radial elements per thread).
 // Variants 4 and 5 stage nothing: one thread per element reads its stencil through L1.
-// Variants 6 and 7 (complex64, even nr): two elements per thread with vector loads (k_band_apply_x2;
-// 128, 64 threads).
-constexpr int kBandVariants = 8;
+// Variants 6, 7, 8 (even nr): two elements per thread with vector loads (k_band_apply_x2 / _x2d;
+// 128, 64, 32 threads).
+constexpr int kBandVariants = 9;
 __host__ __device__ constexpr int band_threads(int v) {
     return v == 0 ? 64 : v == 1 ? 128 : v == 2 ? 128 : v == 3 ? 256 : v == 4 ? 128 : 256;
 }
@@ -574,7 +574,7 @@ static void band_apply_v(const BandOp<T>& op, const void* x, void* y, const Sche
         // (selected by the host only for complex64 operators with split coefficients and even nr;
         // vectors not on a 16-byte boundary take the one-element form)
         if constexpr (sizeof(T) < sizeof(double)) {
-            constexpr int TH = V == 6 ? 128 : 64;
+            constexpr int TH = V == 6 ? 128 : V == 7 ? 64 : 32;
             if (op.slots_lo != nullptr && op.nr % 2 == 0 && ((uintptr_t)x & 15) == 0 && ((uintptr_t)y & 15) == 0) {
                 dim3 grid((op.nr / 2 + TH - 1) / TH, op.nl);
                 launch_pdl(k_band_apply_x2<KB, TH>, grid, dim3(TH), 0, s, op, (const float2*)x, (float2*)y, sched,
@@ -583,7 +583,7 @@ static void band_apply_v(const BandOp<T>& op, const void* x, void* y, const Sche
             }
         }
         if constexpr (sizeof(T) == sizeof(double)) {
-            constexpr int TH = V == 6 ? 128 : 64;
+            constexpr int TH = V == 6 ? 128 : V == 7 ? 64 : 32;
             if (op.nr % 2 == 0) {
                 dim3 grid((op.nr / 2 + TH - 1) / TH, op.nl);
                 launch_pdl(k_band_apply_x2d<KB, TH>, grid, dim3(TH), 0, s, op, (const double2*)x, (double2*)y,
@@ -618,6 +618,7 @@ static void band_apply_kb(const BandOp<T>& op, const void* x, void* y, const Sch
         case 5: band_apply_v<T, KB, 5>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
         case 6: band_apply_v<T, KB, 6>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
         case 7: band_apply_v<T, KB, 7>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
+        case 8: band_apply_v<T, KB, 8>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
         default: band_apply_v<T, KB, 1>(op, x, y, sched, ctrl, scaling, check_broken, s); break;
     }
 }

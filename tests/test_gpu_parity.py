@@ -118,7 +118,7 @@ def test_gram_schmidt_forms_vs_oracle(form, monkeypatch):
     assert st.operator_count == 14 * len(scal) and st.last_basis_size == 14
 
 
-@pytest.mark.parametrize("variant", range(8))
+@pytest.mark.parametrize("variant", range(9))
 @pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
 def test_band_kernel_variants(variant, precision):
     """Every tile shape of the band kernel (staged tiles and the unstaged L1 form) applies the
